@@ -1,0 +1,285 @@
+"""Benchmark of the TCSEM_FDTD time-stepping hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload cfg3]
+
+A "step" is one time step of the hot path (boundary pipeline, fused E/B
+sweep, receiver sampling) over the workload's whole grid; the metric is
+Gcell-steps/s = L*M*N*K / time / 1e9.  Default workload: the 3-D marine
+survey at 256 x 256 x 160 cells (seeded synthetic model in the reference's
+input formats).  With N > 1 (torchrun) every rank runs an independent replica
+on its own GPU; the time is the maximum over ranks and the value the sum of
+cells*steps over ranks.
+
+--impl reference times the CPU implementation of the same path (the FP64 C
+restatement in oracle/, all host threads) on the same workload, on a bounded
+number of steps, rank 0 only.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALGO_BYTES_PER_CELL = {32: 52, 64: 104}  # 7 words read + 6 written per cell and step
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier and max/sum reductions over ranks (gloo; no data-path collective)."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def reduce(self, v, op):
+        if self.world == 1:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX if op == "max" else self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for n, v in zip(names, r[4:8]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        j = json.load(open(p))
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload):
+    """DRAM bytes per fused-sweep launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"fused_sweep_{workload}.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)).get("dram_bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+def make_inputs(workload, rank):
+    from tcsem_fdtd_gb300 import inputs
+
+    d = tempfile.mkdtemp(prefix=f"tcsem_bench_{workload}_r{rank}_")
+    inputs.write_case(inputs.case(workload), d)
+    return d
+
+
+def cpu_reference(args, d, cells):
+    """The oracle (FP64 C, OpenMP) on a bounded number of steps of the same workload."""
+    from oracle.oracle import Oracle, num_threads
+
+    orc = Oracle(d)
+    t0 = time.perf_counter()
+    orc.run(0, max_steps=1)  # first touch of every array, and a per-step estimate
+    per = time.perf_counter() - t0
+    n = int(min(30, max(2, 15.0 / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    _, ran = orc.run(0, max_steps=n)
+    dt = time.perf_counter() - t0
+    return {"value": cells * ran / dt / 1e9, "unit": "Gcell-steps/s", "cores": num_threads(), "kind": "port",
+            "sample": f"{ran} time steps of the {args.workload} workload from a zero state (FP64 C restatement, "
+                      f"{num_threads()} OpenMP threads), {dt:.2f} s"}
+
+
+def run_reference_arm(args, dist):
+    if dist.rank != 0:
+        return 0
+    d = make_inputs(args.workload, 0)
+    from tcsem_fdtd_gb300 import inputs
+
+    c = inputs.case(args.workload)
+    g = inputs.grid_axes(c)
+    cells = g["L"] * g["M"] * g["N"]
+    from oracle.oracle import Oracle, num_threads
+
+    orc = Oracle(d)
+    # bounded sample: W warm-up steps then up to K steps, capped at about a minute of CPU time
+    t0 = time.perf_counter()
+    orc.run(0, max_steps=max(1, min(args.warmup, 3)))
+    per = (time.perf_counter() - t0) / max(1, min(args.warmup, 3))
+    k = max(1, min(args.steps, int(60.0 / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    _, ran = orc.run(0, max_steps=k)
+    dt = time.perf_counter() - t0
+    v = cells * ran / dt / 1e9
+    line = {"metric": "Gcell-steps/s", "value": v, "unit": "Gcell-steps/s", "n_gpus": dist.world, "steps": ran,
+            "warmup": min(args.warmup, 3), "ms_per_step": dt * 1e3 / ran, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": args.workload, "grid": [g["L"], g["M"], g["N"]], "cells": cells},
+            "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": num_threads(), "kind": "port",
+                             "sample": f"{ran} time steps from a zero state, FP64 C restatement of the reference "
+                                       f"path (oracle/tcsem_oracle.c), {num_threads()} OpenMP threads"},
+            "e2e": {"value": v, "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2048)
+    ap.add_argument("--warmup", type=int, default=64)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cfg3")
+    ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference_arm(args, dist)
+        return run_gb300(args, dist)
+    finally:
+        dist.close()
+
+
+def run_gb300(args, dist):
+    from tcsem_fdtd_gb300 import Simulation, build, inputs
+
+    build.build()
+    d = make_inputs(args.workload, dist.rank)
+    c = inputs.case(args.workload)
+    g = inputs.grid_axes(c)
+    cells = g["L"] * g["M"] * g["N"]
+    sim = Simulation(d, precision=args.precision, device=dist.local)
+    nsteps_total = sim.info["nsteps"]
+    K = min(args.steps, nsteps_total - args.warmup)
+    sim.begin(0)
+    sim.advance(args.warmup)  # warm-up steps (graph capture happens here)
+    sim.synchronize()
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        ms = sim.timed_advance(K)
+    dist.barrier()
+    ms_max = dist.reduce(ms, "max")
+    work = dist.reduce(cells * K, "sum")
+    value = work / (ms_max * 1e-3) / 1e9
+    # per-kernel timings on the same stream (events around standalone launches)
+    _, ms_sweep, ms_bnd = sim.time_steps(0, 64)
+    algo = ALGO_BYTES_PER_CELL[args.precision] * cells
+    peak, peak_kind = measured_peak()
+    achieved = algo / (ms_sweep * 1e-3) / 1e9
+    # end to end through the C ABI: files -> device -> all steps -> traces on the host
+    t0 = time.perf_counter()
+    with Simulation(d, precision=args.precision, device=dist.local) as s2:
+        tr = s2.run(0)
+        info2 = s2.info
+    e2e_s = time.perf_counter() - t0
+    e2e_s = dist.reduce(e2e_s, "max")
+    e2e_val = dist.reduce(cells * info2["nsteps"], "sum") / e2e_s / 1e9
+    h2d = info2["device_bytes"]
+    d2h = tr.nbytes
+    sim.close()
+    line = {
+        "metric": "Gcell-steps/s", "value": value, "unit": "Gcell-steps/s", "n_gpus": dist.world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "grid": [g["L"], g["M"], g["N"]], "cells": cells,
+                   "plane": [info2["L1"], info2["M1"]], "receivers": info2["NRx"],
+                   "steps_per_run": nsteps_total, "parallelism": f"replicas{dist.world}",
+                   "l2": "working set 13 x %.0f MB volume arrays > 129 MB L2, no flush needed"
+                         % (cells * 4 * 1.13 / 1e6)},
+        "gpu_launches": K * 6 + math.ceil(K / 64),
+        "roofline": {"bound": "hbm", "kernel": "k_fused_sweep", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(args.workload), "ms_per_launch": ms_sweep,
+                     "algo_bytes_per_launch": algo, "boundary_ms_per_step": ms_bnd},
+        "e2e": {"value": e2e_val, "unit": "Gcell-steps/s", "h2d_bytes_per_step": h2d / info2["nsteps"],
+                "d2h_bytes_per_step": d2h / info2["nsteps"],
+                "what": "tcsem_open_dir (files, host setup, uploads) + tcsem_run of all %d steps + traces to host"
+                        % info2["nsteps"], "seconds": e2e_s},
+        "clocks": clk.summary(),
+    }
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_reference(args, d, cells)
+        except Exception as e:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

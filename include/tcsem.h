@@ -1,0 +1,129 @@
+/*
+ * tcsem.h -- C ABI of the GB300-native TCSEM_FDTD time-stepping path.
+ *
+ * One handle (tcsem_sim) holds one survey (model, grid, receivers, all
+ * transmitters) and owns all of its device memory; handles are independent
+ * (no global or __constant__ state), each works on its own CUDA stream, and a
+ * handle must be used from one host thread at a time.  Every entry point
+ * returns a tcsem_status; no entry point exits the process or reads stdin.
+ *
+ * Field arrays exchanged with the host use the reference's layout (FTDT.h:62-74,
+ * prepare_free_mem.cu:63-81), x fastest:
+ *   Ex[N+1][M+1][L]  Ey[N+1][M][L+1]  Ez[N][M+1][L+1]
+ *   Bx[N][M][L+1]    By[N][M+1][L]    Bz[N+1][M][L]
+ *   BxAir[M][L+1]    ByAir[M+1][L]    Con[N][M][L]
+ * Traces are double [nr][NComp][Nt] like the Tx<k>.bout payload (main.cu:278-292).
+ */
+#ifndef TCSEM_H_INCLUDED
+#define TCSEM_H_INCLUDED
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TCSEM_OK = 0,
+    TCSEM_ERR_IO = 1,       /* an input or output file could not be opened/written */
+    TCSEM_ERR_PARSE = 2,    /* malformed input file */
+    TCSEM_ERR_INVALID = 3,  /* inconsistent model/survey or bad argument */
+    TCSEM_ERR_CUDA = 4,     /* CUDA runtime error or no usable GPU */
+    TCSEM_ERR_NOMEM = 5,    /* device or host allocation failed */
+    TCSEM_ERR_STATE = 6,    /* call not valid in the handle's current state */
+    TCSEM_ERR_NUMERIC = 7   /* a non-finite value appeared in the fields */
+} tcsem_status;
+
+enum { TCSEM_FP32 = 32, TCSEM_FP64 = 64 };
+
+typedef struct tcsem_sim tcsem_sim_t;
+
+enum {
+    TCSEM_EX = 0, TCSEM_EY = 1, TCSEM_EZ = 2, TCSEM_BX = 3, TCSEM_BY = 4, TCSEM_BZ = 5,
+    TCSEM_BXAIR = 6, TCSEM_BYAIR = 7, TCSEM_CON = 8
+};
+
+typedef struct {
+    int precision;        /* TCSEM_FP32 (default) or TCSEM_FP64 */
+    int device;           /* CUDA device ordinal, default 0 */
+    int fix_dual_bipole;  /* 1: inject the second bipole of ort=5 at its own cells (default 0 = as the reference) */
+    int graph_steps;      /* steps per captured CUDA graph, 0 = default (even numbers only) */
+    int reserved[4];
+} tcsem_opts;
+
+typedef struct {
+    int L, M, N;          /* cells in x, y, z */
+    int L1, M1;           /* uniform continuation plane */
+    int NRx, NTx, Nt, NComp, nefcmp;
+    long nsteps;          /* time steps of one transmitter run */
+    int precision;
+    size_t device_bytes;  /* device memory held by the handle */
+} tcsem_info;
+
+/* Opening a survey.  tcsem_open_dir reads FDTD_setup.in, Cond.bin, Receiver.in
+ * and Transmitter.in from `dir` -- the reference reads them from its working
+ * directory (ModelingSetup.cpp:43-209, LoadRxTxPos.cpp:43-200). */
+void tcsem_default_opts(tcsem_opts *opts);
+tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t **out);
+tcsem_status tcsem_close(tcsem_sim_t *sim);
+const char *tcsem_last_error(const tcsem_sim_t *sim); /* message of the last failed call on `sim` */
+const char *tcsem_open_error(void);                   /* message of the last failed open (per thread) */
+tcsem_status tcsem_get_info(const tcsem_sim_t *sim, tcsem_info *out);
+
+/* Whole runs: the transmitter loop body of main.cu:195-298 (with the state
+ * reset per transmitter that the reference omits).  traces: [nr][NComp][Nt]. */
+tcsem_status tcsem_run(tcsem_sim_t *sim, int itx, double *traces);
+tcsem_status tcsem_write_bout(tcsem_sim_t *sim, int itx, const double *traces, const char *path);
+
+/* Stepwise form of tcsem_run: begin resets the fields for transmitter itx;
+ * advance runs exactly min(nsteps, steps left) more steps (whole blocks as
+ * replays of one captured CUDA graph, the rest launched directly); done is set
+ * once the last step has run; traces can be read at any time. */
+tcsem_status tcsem_begin(tcsem_sim_t *sim, int itx);
+tcsem_status tcsem_advance(tcsem_sim_t *sim, long nsteps, int *done);
+tcsem_status tcsem_get_traces(tcsem_sim_t *sim, double *traces);
+tcsem_status tcsem_synchronize(tcsem_sim_t *sim);
+
+/* Per-stage entry points, the seam of FTDT.h:291-344.  They act on the
+ * handle's current fields like the reference's functions act on DArrays:
+ *   tcsem_upcontinuation   <- UpContinuation_gpu (UpContinuation_gpu.cu:166)
+ *   tcsem_electric_field   <- ElectricalField    (ElectricalFiled.cu:478)
+ *   tcsem_bderivate        <- Bderivate          (Bderivate.cu:269)
+ *   tcsem_rx_sample        <- EFXInterp/BFXInterp (EFInterp2Rx.cu:410-470), into slot 0 or 1
+ *   tcsem_fused_step       <- ElectricalField followed by Bderivate, as one fused sweep */
+tcsem_status tcsem_select_tx(tcsem_sim_t *sim, int itx);
+tcsem_status tcsem_upcontinuation(tcsem_sim_t *sim);
+tcsem_status tcsem_electric_field(tcsem_sim_t *sim, double lambda, double dt, double wave);
+tcsem_status tcsem_bderivate(tcsem_sim_t *sim, double dt);
+tcsem_status tcsem_fused_step(tcsem_sim_t *sim, double lambda, double dt, double dt_b, double wave);
+tcsem_status tcsem_rx_sample(tcsem_sim_t *sim, int efield, int slot, double *values /* [NComp][nr] slot image */);
+
+/* Host <-> device field access in the reference layout (comp = TCSEM_EX ...). */
+tcsem_status tcsem_get_field(tcsem_sim_t *sim, int comp, double *host);
+tcsem_status tcsem_set_field(tcsem_sim_t *sim, int comp, const double *host);
+tcsem_status tcsem_field_size(const tcsem_sim_t *sim, int comp, size_t *count);
+
+/* Source waveform of SourceWave.cpp:8-58 (what the reference writes to
+ * testwaveform.dat): nsrc = n1/2, arrays of 2*nsrc+1 entries (may be NULL). */
+tcsem_status tcsem_get_waveform(const tcsem_sim_t *sim, int *nsrc, double *t, double *dt, double *wave);
+
+/* Host-side schedule, for inspection: per step dt1, dt2, lambda and source
+ * amplitude (main.cu:212-260); each array may be NULL; `cap` entries at most. */
+tcsem_status tcsem_get_schedule(const tcsem_sim_t *sim, double *dt1, double *dt2, double *lambda, double *wave, long cap);
+
+/* Device time (CUDA events on the handle's stream) of tcsem_advance(nsteps)
+ * from the current state; the state advances like tcsem_advance. */
+tcsem_status tcsem_timed_advance(tcsem_sim_t *sim, long nsteps, double *ms);
+
+/* Timing of the captured step loop on the handle's stream: runs `nsteps`
+ * steps of transmitter itx from a fresh state and reports the elapsed device
+ * time (CUDA events), plus, if non-NULL, the time of the fused volume sweep
+ * and of the boundary pipeline measured separately with events. */
+tcsem_status tcsem_time_steps(tcsem_sim_t *sim, int itx, long nsteps, double *ms_total, double *ms_sweep,
+                              double *ms_boundary);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCSEM_H_INCLUDED */

@@ -1,0 +1,229 @@
+"""Python mirror of the C ABI in include/tcsem.h (ctypes, no torch types).
+
+The library is the in-tree ``libtcsem.so`` built by :mod:`tcsem_fdtd_gb300.build`.
+There is no CPU path: if the library or a CUDA device is missing, opening a
+simulation raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libtcsem.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "tcsem.h")
+
+STATUS = {0: "OK", 1: "IO", 2: "PARSE", 3: "INVALID", 4: "CUDA", 5: "NOMEM", 6: "STATE", 7: "NUMERIC"}
+COMP = {"Ex": 0, "Ey": 1, "Ez": 2, "Bx": 3, "By": 4, "Bz": 5, "BxAir": 6, "ByAir": 7, "Con": 8}
+
+
+class TcsemError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"tcsem {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("device", C.c_int), ("fix_dual_bipole", C.c_int), ("graph_steps", C.c_int),
+                ("reserved", C.c_int * 4)]
+
+
+class Info(C.Structure):
+    _fields_ = [("L", C.c_int), ("M", C.c_int), ("N", C.c_int), ("L1", C.c_int), ("M1", C.c_int),
+                ("NRx", C.c_int), ("NTx", C.c_int), ("Nt", C.c_int), ("NComp", C.c_int), ("nefcmp", C.c_int),
+                ("nsteps", C.c_long), ("precision", C.c_int), ("device_bytes", C.c_size_t)]
+
+
+def declared_functions():
+    """Names of the functions that include/tcsem.h declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tcsem_[a-z0-9_]+)\s*\(", text)))
+
+
+_lib = None
+
+
+def library():
+    """Load libtcsem.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OSError(f"{LIB_PATH} is missing: build it with `python -m tcsem_fdtd_gb300.build`")
+    L = C.CDLL(LIB_PATH)
+    vp, dp, ip, i, d, l_ = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int, C.c_double, C.c_long
+    sig = {
+        "tcsem_default_opts": (None, [C.POINTER(Opts)]),
+        "tcsem_open_dir": (i, [C.c_char_p, C.POINTER(Opts), C.POINTER(vp)]),
+        "tcsem_close": (i, [vp]),
+        "tcsem_last_error": (C.c_char_p, [vp]),
+        "tcsem_open_error": (C.c_char_p, []),
+        "tcsem_get_info": (i, [vp, C.POINTER(Info)]),
+        "tcsem_run": (i, [vp, i, dp]),
+        "tcsem_write_bout": (i, [vp, i, dp, C.c_char_p]),
+        "tcsem_begin": (i, [vp, i]),
+        "tcsem_advance": (i, [vp, l_, ip]),
+        "tcsem_get_traces": (i, [vp, dp]),
+        "tcsem_synchronize": (i, [vp]),
+        "tcsem_select_tx": (i, [vp, i]),
+        "tcsem_upcontinuation": (i, [vp]),
+        "tcsem_electric_field": (i, [vp, d, d, d]),
+        "tcsem_bderivate": (i, [vp, d]),
+        "tcsem_fused_step": (i, [vp, d, d, d, d]),
+        "tcsem_rx_sample": (i, [vp, i, i, dp]),
+        "tcsem_get_field": (i, [vp, i, dp]),
+        "tcsem_set_field": (i, [vp, i, dp]),
+        "tcsem_field_size": (i, [vp, i, C.POINTER(C.c_size_t)]),
+        "tcsem_get_waveform": (i, [vp, ip, dp, dp, dp]),
+        "tcsem_get_schedule": (i, [vp, dp, dp, dp, dp, l_]),
+        "tcsem_time_steps": (i, [vp, i, l_, dp, dp, dp]),
+        "tcsem_timed_advance": (i, [vp, l_, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Simulation:
+    """One survey on one GPU: the handle of include/tcsem.h."""
+
+    def __init__(self, directory, precision=32, device=0, fix_dual_bipole=False, graph_steps=0):
+        L = library()
+        o = Opts()
+        L.tcsem_default_opts(C.byref(o))
+        o.precision, o.device, o.fix_dual_bipole, o.graph_steps = precision, device, int(fix_dual_bipole), graph_steps
+        h = C.c_void_p()
+        st = L.tcsem_open_dir(os.fsencode(directory), C.byref(o), C.byref(h))
+        if st != 0:
+            raise TcsemError(st, L.tcsem_open_error().decode())
+        self._h = h
+        inf = Info()
+        L.tcsem_get_info(h, C.byref(inf))
+        self.info = {f: getattr(inf, f) for f, _ in Info._fields_}
+        self.precision = precision
+
+    # ------------------------------------------------------------------ plumbing
+    def _check(self, st):
+        if st != 0:
+            raise TcsemError(st, library().tcsem_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().tcsem_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --------------------------------------------------------------- whole runs
+    def run(self, itx=0, nr=None):
+        """All steps of transmitter itx; returns traces [nr][NComp][Nt]."""
+        i = self.info
+        buf = np.zeros(i["NRx"] * i["NComp"] * i["Nt"])
+        self._check(library().tcsem_run(self._h, itx, _dptr(buf)))
+        n = nr if nr is not None else i["NRx"]
+        return buf[: n * i["NComp"] * i["Nt"]].reshape(n, i["NComp"], i["Nt"])
+
+    def write_bout(self, itx, traces, path):
+        t = np.ascontiguousarray(traces, dtype=np.float64)
+        self._check(library().tcsem_write_bout(self._h, itx, _dptr(t), os.fsencode(path)))
+
+    def begin(self, itx=0):
+        self._check(library().tcsem_begin(self._h, itx))
+
+    def advance(self, nsteps):
+        done = C.c_int(0)
+        self._check(library().tcsem_advance(self._h, nsteps, C.byref(done)))
+        return bool(done.value)
+
+    def traces(self, nr):
+        i = self.info
+        buf = np.zeros(i["NRx"] * i["NComp"] * i["Nt"])
+        self._check(library().tcsem_get_traces(self._h, _dptr(buf)))
+        return buf[: nr * i["NComp"] * i["Nt"]].reshape(nr, i["NComp"], i["Nt"])
+
+    def synchronize(self):
+        self._check(library().tcsem_synchronize(self._h))
+
+    # -------------------------------------------------------------- stage seam
+    def select_tx(self, itx):
+        self._check(library().tcsem_select_tx(self._h, itx))
+
+    def upcontinuation(self):
+        self._check(library().tcsem_upcontinuation(self._h))
+
+    def electric_field(self, lam, dt, wave):
+        self._check(library().tcsem_electric_field(self._h, lam, dt, wave))
+
+    def bderivate(self, dt):
+        self._check(library().tcsem_bderivate(self._h, dt))
+
+    def fused_step(self, lam, dt, dtb, wave):
+        self._check(library().tcsem_fused_step(self._h, lam, dt, dtb, wave))
+
+    def rx_sample(self, efield, slot, nr):
+        out = np.zeros(self.info["NComp"] * self.info["NRx"])
+        self._check(library().tcsem_rx_sample(self._h, int(bool(efield)), slot, _dptr(out)))
+        return out[: self.info["NComp"] * nr].reshape(self.info["NComp"], nr)
+
+    # ------------------------------------------------------------ field access
+    def field_shape(self, name):
+        L, M, N = self.info["L"], self.info["M"], self.info["N"]
+        return {"Ex": (N + 1, M + 1, L), "Ey": (N + 1, M, L + 1), "Ez": (N, M + 1, L + 1), "Bx": (N, M, L + 1),
+                "By": (N, M + 1, L), "Bz": (N + 1, M, L), "BxAir": (M, L + 1), "ByAir": (M + 1, L),
+                "Con": (N, M, L)}[name]
+
+    def get(self, name):
+        out = np.zeros(self.field_shape(name))
+        self._check(library().tcsem_get_field(self._h, COMP[name], _dptr(out)))
+        return out
+
+    def set(self, name, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.shape == self.field_shape(name)
+        self._check(library().tcsem_set_field(self._h, COMP[name], _dptr(a)))
+
+    def waveform(self):
+        n = C.c_int(0)
+        self._check(library().tcsem_get_waveform(self._h, C.byref(n), None, None, None))
+        t, dt, w = (np.zeros(2 * n.value + 1) for _ in range(3))
+        self._check(library().tcsem_get_waveform(self._h, C.byref(n), _dptr(t), _dptr(dt), _dptr(w)))
+        return t, dt, w
+
+    def schedule(self):
+        n = self.info["nsteps"]
+        a = [np.zeros(n) for _ in range(4)]
+        self._check(library().tcsem_get_schedule(self._h, *[_dptr(x) for x in a], n))
+        return dict(dt1=a[0], dt2=a[1], lam=a[2], wave=a[3], nsteps=n)
+
+    def timed_advance(self, nsteps):
+        """Advance `nsteps` steps; returns their device time in ms (CUDA events on the handle's stream)."""
+        ms = C.c_double()
+        self._check(library().tcsem_timed_advance(self._h, nsteps, C.byref(ms)))
+        return ms.value
+
+    def time_steps(self, itx, nsteps):
+        """Device time (ms) of `nsteps` captured steps, and of one sweep / one boundary pass."""
+        tot, sw, bn = C.c_double(), C.c_double(), C.c_double()
+        self._check(library().tcsem_time_steps(self._h, itx, nsteps, C.byref(tot), C.byref(sw), C.byref(bn)))
+        return tot.value, sw.value, bn.value

@@ -1,0 +1,70 @@
+"""Build the CUDA library and the drop-in executable in-tree with nvcc.
+
+Outputs (git-ignored):
+  tcsem_fdtd_gb300/libtcsem.so   -- the C-ABI library of include/tcsem.h
+  tcsem_fdtd_gb300/tcsem_fdtd    -- drop-in replacement of the reference executable
+Every translation unit is compiled for sm_103a only, in parallel.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libtcsem.so")
+CLI = os.path.join(PKG, "tcsem_fdtd")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["setup.cpp", "volume.cu", "boundary.cu", "rx.cu", "sim.cu"]
+
+
+def nvcc():
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    return cand if os.path.exists(cand) else (shutil.which("nvcc") or "nvcc")
+
+
+def _flags():
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
+                   "-I", CSRC, "--expt-relaxed-constexpr"]
+
+
+def _compile(src, verbose):
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    path = os.path.join(CSRC, src)
+    deps = [path] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    deps.append(os.path.join(ROOT, "include", "tcsem.h"))
+    if os.path.exists(obj) and all(os.path.getmtime(obj) > os.path.getmtime(d) for d in deps):
+        return obj
+    cmd = [nvcc()] + _flags() + ["-c", path, "-o", obj]
+    if src.endswith(".cpp"):
+        cmd[1:1] = ["-x", "cu"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def build(verbose=False, jobs=None):
+    os.makedirs(BUILD, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(len(SOURCES), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"], check=True)
+        os.replace(tmp, LIB)
+    cli_obj = _compile("cli.cpp", verbose)
+    if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(LIB), os.path.getmtime(cli_obj)):
+        subprocess.run([nvcc()] + ARCH + ["-o", CLI, cli_obj, "-L", PKG, "-ltcsem", "-Xlinker", "-rpath=$ORIGIN"],
+                       check=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,78 @@
+// tcsem_fdtd: drop-in replacement of the reference executable TCSEM_FDTD_GPU.
+// Reads FDTD_setup.in, Cond.bin, Receiver.in and Transmitter.in from the
+// working directory (or the directory given as the first argument), runs every
+// transmitter and writes Tx<k>.bout and testwaveform.dat like main.cu:58-324.
+// Options: --fp64 (double-precision build mode), --device N, --fix-dual-bipole.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tcsem.h"
+
+int main(int argc, char **argv) {
+    std::string dir = ".";
+    tcsem_opts o;
+    tcsem_default_opts(&o);
+    for (int a = 1; a < argc; a++) {
+        if (!std::strcmp(argv[a], "--fp64")) o.precision = TCSEM_FP64;
+        else if (!std::strcmp(argv[a], "--fix-dual-bipole")) o.fix_dual_bipole = 1;
+        else if (!std::strcmp(argv[a], "--device") && a + 1 < argc) o.device = std::atoi(argv[++a]);
+        else if (argv[a][0] != '-') dir = argv[a];
+        else { std::fprintf(stderr, "usage: tcsem_fdtd [dir] [--fp64] [--device N] [--fix-dual-bipole]\n"); return 2; }
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    tcsem_sim_t *sim = nullptr;
+    tcsem_status st = tcsem_open_dir(dir.c_str(), &o, &sim);
+    if (st != TCSEM_OK) {
+        std::fprintf(stderr, "Error: unable to load the setup or model (%d): %s\n", (int)st, tcsem_open_error());
+        return 1;
+    }
+    std::printf("The model is initialized successfully!\n");
+    tcsem_info info;
+    tcsem_get_info(sim, &info);
+    std::printf("time iteration =%ld\n", info.nsteps);
+    {  // testwaveform.dat, SourceWave.cpp:60-71
+        int nsrc = 0;
+        tcsem_get_waveform(sim, &nsrc, nullptr, nullptr, nullptr);
+        std::vector<double> t(2 * nsrc + 1), dt(2 * nsrc + 1), w(2 * nsrc + 1);
+        tcsem_get_waveform(sim, &nsrc, t.data(), dt.data(), w.data());
+        std::string p = dir + "/testwaveform.dat";
+        FILE *f = std::fopen(p.c_str(), "wb");
+        if (f) {
+            std::fwrite(&nsrc, sizeof(int), 1, f);
+            std::fwrite(t.data(), sizeof(double), t.size(), f);
+            std::fwrite(dt.data(), sizeof(double), dt.size(), f);
+            std::fwrite(w.data(), sizeof(double), w.size(), f);
+            std::fclose(f);
+        }
+    }
+    auto tg = std::chrono::steady_clock::now();
+    int rc = 0;
+    // traces of one transmitter fit in NRx*NComp*Nt doubles
+    std::vector<double> traces((size_t)info.NRx * info.NComp * info.Nt);
+    for (int itx = 0; itx < info.NTx; itx++) {
+        std::printf("start to model the EM field generated by Tx %d\n", itx + 1);
+        st = tcsem_run(sim, itx, traces.data());
+        if (st != TCSEM_OK) {
+            std::fprintf(stderr, "Error in transmitter %d (%d): %s\n", itx + 1, (int)st, tcsem_last_error(sim));
+            rc = 1;
+            continue;
+        }
+        char name[64];
+        std::snprintf(name, sizeof name, "/Tx%d.bout", itx + 1);
+        st = tcsem_write_bout(sim, itx, traces.data(), (dir + name).c_str());
+        if (st != TCSEM_OK) {
+            std::fprintf(stderr, "Error writing %s: %s\n", name + 1, tcsem_last_error(sim));
+            rc = 1;
+        }
+        std::printf("end of time iteration for Tx %d\n", itx + 1);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    std::printf("FDTD modleing completed, runtime=%8.1f sec.\n", std::chrono::duration<double>(t1 - t0).count());
+    std::printf("Pure GPU runtime=%8.1f sec.\n", std::chrono::duration<double>(t1 - tg).count());
+    tcsem_close(sim);
+    return rc;
+}

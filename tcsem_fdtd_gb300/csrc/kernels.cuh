@@ -1,0 +1,90 @@
+// Device-side data layout and kernel entry points of the TCSEM path.
+//
+// HBM layout.  All seven volume arrays (Ex, Ey, Ez, Bx, By, Bz and the
+// conductivity) share one padded geometry so that a single index expression
+// addresses any of them and neighbouring components line up in memory:
+//   x (fastest): i in [-4, XP-4), row pitch XP = round_up(L + 6, 32) elements,
+//                so i = 0 starts on a 128-byte boundary;
+//   y          : j in [-1, M]    (YP = M + 2 rows per plane);
+//   z          : k in [-1, N]    (N + 2 planes).
+// Cells outside a component's update range stay zero for the life of the run.
+// Plane k = -1 of Bx and By holds the air-interface fields BxAir/ByAir that
+// the boundary pipeline writes each step, plane k = -1 of the conductivity is
+// the air (0 S/m), and plane N of Ex/Ey/Bz is the zero bottom -- so the
+// kernels need no special case for the top or bottom plane.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace tcsem {
+
+struct Geom {
+    int L, M, N;
+    int XP, YP;
+    long long PS;  // plane stride XP*YP
+    __host__ __device__ long long at(int i, int j, int k) const {
+        return ((long long)(k + 1) * YP + (j + 1)) * XP + (i + 4);
+    }
+    __host__ __device__ long long total() const { return PS * (long long)(N + 2); }
+};
+
+inline Geom make_geom(int L, int M, int N) {
+    Geom g;
+    g.L = L; g.M = M; g.N = N;
+    g.XP = ((L + 6 + 31) / 32) * 32;
+    g.YP = M + 2;
+    g.PS = (long long)g.XP * g.YP;
+    return g;
+}
+
+// per-axis tables: sizes and reciprocals of sizes / summed sizes
+template <typename T> struct Axis {
+    const T *dxk, *dyk, *dzk;  // cell sizes as the reference kernels evaluate them
+    const T *rdx, *rdy, *rdz;  // 1/dxk ...
+    const T *rdx2, *rdy2;      // 1/(dxk[i-1]+dxk[i]), 1/(dyk[j-1]+dyk[j]) (index 0 unused)
+    const T *rdzs;             // 1/(dzk[k-1]+dzk[k]), k=0: 1/(2 dzk[0])
+};
+
+template <typename T> struct FieldSet {
+    T *ex, *ey, *ez, *bx, *by, *bz;
+};
+
+// scalars of one time step
+template <typename T> struct StepScalars {
+    T lam2;  // 2*lambda (gamma term of DuFort-Frankel)
+    T dt;    // E step dt1
+    T c4;    // 4*dt/mu0
+    T dtb;   // B step 0.5*(dt1+dt2)
+    T wave;  // source amplitude of this step (0 once the source is off)
+};
+
+// source segments (at most kMaxSeg per transmitter), see setup.h
+constexpr int kMaxSeg = 6;
+template <typename T> struct SourceTable {
+    int nseg;
+    int comp[kMaxSeg], i[kMaxSeg], j[kMaxSeg], k[kMaxSeg], count[kMaxSeg], off[kMaxSeg];
+    const T *coef;  // gain already folded in: value = wave * coef[off + q]
+};
+
+// which step of a captured block a kernel belongs to: step = *base + off;
+// kernels do nothing once step >= nsteps.  base == nullptr: always run.
+struct StepGate {
+    const int *base;
+    int off;
+    long nsteps;
+    __device__ __forceinline__ long step() const { return (long)*base + off; }
+};
+
+// ----------------------------------------------------------------- launchers
+// volume.cu
+template <typename T>
+void launch_update_e(const Geom &g, FieldSet<T> f, const T *con, const Axis<T> &ax, StepScalars<T> s,
+                     const SourceTable<T> &src, cudaStream_t st);
+template <typename T>
+void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, cudaStream_t st);
+template <typename T>
+void launch_fused_sweep(const Geom &g, FieldSet<T> in, FieldSet<T> out, const T *con, const Axis<T> &ax,
+                        StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
+                        const SourceTable<T> &src, cudaStream_t st);
+
+}  // namespace tcsem

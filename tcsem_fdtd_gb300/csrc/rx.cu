@@ -1,0 +1,81 @@
+// Receiver sampling (EFInterp2Rx.cu): 4x4x4 natural-spline interpolation of
+// the staggered components to the receivers, stored into one of two slots,
+// and linear interpolation in time between the slots at the sampling times.
+//
+// The host decides, per step, which slot the current E (B) field goes to and
+// which samples are produced (EFInterp2Rx.cu:472-585); that plan is a device
+// table here so the kernel can run inside captured step blocks.  A sample
+// produced in a step uses slot 0 (written in an earlier step) and the slot-1
+// value being computed, so the time interpolation is fused into the spatial
+// pass and needs no grid-wide synchronisation.
+#include "kernels.cuh"
+#include "rx.cuh"
+
+namespace tcsem {
+
+template <typename T>
+__device__ __forceinline__ T stencil_value(const RxDev<T> &rd, const FieldSet<T> &f, int s, const Geom &g) {
+    const int comp = rd.comp[s];
+    const T *F = comp == 0 ? f.ex : comp == 1 ? f.ey : comp == 2 ? f.ez : comp == 3 ? f.bx : comp == 4 ? f.by : f.bz;
+    const T *w = rd.w + (size_t)s * 12;
+    const long long base = rd.base[s];
+    T v = T(0);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        T vy = T(0);
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const T *row = F + base + (long long)c * g.PS + (long long)b * g.XP;
+            T vx = w[0] * row[0] + w[1] * row[1] + w[2] * row[2] + w[3] * row[3];
+            vy += w[4 + b] * vx;
+        }
+        v += w[8 + c] * vy;
+    }
+    return v;
+}
+
+template <typename T>
+__global__ void k_rx(RxDev<T> rd, FieldSet<T> f, Geom g, StepGate gate, RxAction act) {
+    if (gate.base) {
+        const long st = gate.step();
+        if (st >= gate.nsteps) return;
+        const StepEntryActs &a = rd.acts[st];
+        act.e_slot = a.e_slot; act.e_first = a.e_first; act.e_count = a.e_count;
+        act.b_slot = a.b_slot; act.b_first = a.b_first; act.b_count = a.b_count;
+    }
+    const int nr = rd.nr, NC = rd.NComp, ne = rd.nefcmp;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= NC * nr) return;
+    const int p = idx / nr, r = idx % nr;  // slot image position [p][r]
+    const bool efield = p < ne;
+    const int slot = efield ? act.e_slot : act.b_slot;
+    if (slot < 0) return;
+    const T v = stencil_value(rd, f, idx, g);
+    rd.ef0[(size_t)slot * NC * nr + idx] = v;
+    const int first = efield ? act.e_first : act.b_first, count = efield ? act.e_count : act.b_count;
+    const T *l1 = efield ? rd.e_l1 : rd.b_l1;
+    if (slot == 1) {  // EFTimeInterp / BFTimeInterp, EFInterp2Rx.cu:380-407
+        const T v0 = rd.ef0[idx];
+        for (int s = first; s < first + count; s++)
+            rd.efs[((size_t)r * NC + p) * rd.Nt + s] = (T(1) - l1[s]) * v0 + l1[s] * v;
+    }
+}
+
+template <typename T>
+__global__ void k_advance(int *base, int by) {
+    *base += by;
+}
+
+template <typename T>
+void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const Geom &g, StepGate gate, RxAction act, cudaStream_t st) {
+    int n = rd.NComp * rd.nr;
+    if (n == 0) return;
+    k_rx<T><<<(n + 127) / 128, 128, 0, st>>>(rd, f, g, gate, act);
+}
+
+void launch_advance(int *base, int by, cudaStream_t st) { k_advance<float><<<1, 1, 0, st>>>(base, by); }
+
+template void launch_rx<float>(const RxDev<float> &, FieldSet<float>, const Geom &, StepGate, RxAction, cudaStream_t);
+template void launch_rx<double>(const RxDev<double> &, FieldSet<double>, const Geom &, StepGate, RxAction, cudaStream_t);
+
+}  // namespace tcsem

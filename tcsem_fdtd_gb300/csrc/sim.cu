@@ -1,0 +1,790 @@
+// Simulation handle and the C ABI of include/tcsem.h.
+//
+// A handle owns, on one device and one stream:
+//   * two field sets (ping-pong) in the padded layout of kernels.cuh, plus the
+//     conductivity -- 13 volume arrays;
+//   * the boundary pipeline's operators and scratch (boundary.cuh);
+//   * the per-step table (scalars + receiver plan) of the whole run, so a
+//     block of steps is one CUDA graph that is captured once and replayed;
+//   * the receiver stencils, slots and traces of the selected transmitter.
+// The step loop of main.cu:219-273 becomes: graph launch per block of
+// `graph_steps` steps, each step = boundary (4 kernels) -> fused sweep ->
+// receiver kernel, followed by one counter advance per block.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "boundary.cuh"
+#include "kernels.cuh"
+#include "rx.cuh"
+#include "setup.h"
+#include "tcsem.h"
+
+namespace tcsem {
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            throw Error(e_ == cudaErrorMemoryAllocation ? TCSEM_ERR_NOMEM : TCSEM_ERR_CUDA,             \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+    } while (0)
+
+struct DevMem {
+    void *p = nullptr;
+    size_t n = 0;
+    DevMem() = default;
+    DevMem(const DevMem &) = delete;
+    DevMem &operator=(const DevMem &) = delete;
+    ~DevMem() { if (p) cudaFree(p); }
+    void alloc(size_t bytes) {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = bytes;
+        if (bytes) CK(cudaMalloc(&p, bytes));
+    }
+    template <class U> U *as() const { return reinterpret_cast<U *>(p); }
+};
+
+static FFTPlan make_plan(int n) {
+    FFTPlan P{};
+    P.n = n;
+    int m = n;
+    while (m % 8 == 0) { P.radix[P.nst++] = 8; m /= 8; }
+    while (m % 4 == 0) { P.radix[P.nst++] = 4; m /= 4; }
+    while (m % 2 == 0) { P.radix[P.nst++] = 2; m /= 2; }
+    for (int p = 3; m > 1; p += 2)
+        while (m % p == 0) { P.radix[P.nst++] = p; m /= p; }
+    return P;
+}
+
+// ---------------------------------------------------------------- base class
+struct SimBase {
+    Model model;
+    Schedule sched;
+    tcsem_opts opts{};
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int itx = -1;
+    bool begun = false;
+    long step = 0;
+    size_t dev_bytes = 0;
+    virtual ~SimBase() {}
+    virtual void init() = 0;
+    virtual void select(int itx) = 0;
+    virtual void begin(int itx) = 0;
+    virtual void advance(long n, int *done) = 0;
+    virtual void traces(double *out) = 0;
+    virtual void upcontinuation() = 0;
+    virtual void electric_field(double lam, double dt, double wave) = 0;
+    virtual void bderivate(double dt) = 0;
+    virtual void fused_step(double lam, double dt, double dtb, double wave) = 0;
+    virtual void rx_sample(int efield, int slot, double *values) = 0;
+    virtual void get_field(int comp, double *h) = 0;
+    virtual void set_field(int comp, const double *h) = 0;
+    virtual void time_steps(int itx, long n, double *tot, double *sweep, double *bnd) = 0;
+    virtual void timed_advance(long n, double *ms) = 0;
+    size_t field_count(int comp) const {
+        size_t L = model.L, M = model.M, N = model.N;
+        switch (comp) {
+        case TCSEM_EX: return L * (M + 1) * (N + 1);
+        case TCSEM_EY: return (L + 1) * M * (N + 1);
+        case TCSEM_EZ: return (L + 1) * (M + 1) * N;
+        case TCSEM_BX: return (L + 1) * M * N;
+        case TCSEM_BY: return L * (M + 1) * N;
+        case TCSEM_BZ: return L * M * (N + 1);
+        case TCSEM_BXAIR: return (L + 1) * M;
+        case TCSEM_BYAIR: return L * (M + 1);
+        case TCSEM_CON: return L * M * N;
+        }
+        throw Error(TCSEM_ERR_INVALID, "unknown field component");
+    }
+    // extents (nx, ny, nz, z0) of a component in the reference layout
+    void extents(int comp, int &nx, int &ny, int &nz, int &z0) const {
+        int L = model.L, M = model.M, N = model.N;
+        z0 = 0;
+        switch (comp) {
+        case TCSEM_EX: nx = L; ny = M + 1; nz = N + 1; break;
+        case TCSEM_EY: nx = L + 1; ny = M; nz = N + 1; break;
+        case TCSEM_EZ: nx = L + 1; ny = M + 1; nz = N; break;
+        case TCSEM_BX: nx = L + 1; ny = M; nz = N; break;
+        case TCSEM_BY: nx = L; ny = M + 1; nz = N; break;
+        case TCSEM_BZ: nx = L; ny = M; nz = N + 1; break;
+        case TCSEM_BXAIR: nx = L + 1; ny = M; nz = 1; z0 = -1; break;
+        case TCSEM_BYAIR: nx = L; ny = M + 1; nz = 1; z0 = -1; break;
+        case TCSEM_CON: nx = L; ny = M; nz = N; break;
+        default: throw Error(TCSEM_ERR_INVALID, "unknown field component");
+        }
+    }
+};
+
+// ---------------------------------------------------------------- typed impl
+template <typename T> struct SimImpl : SimBase {
+    Geom g{};
+    DevMem fld[2][6], con;
+    DevMem axis_mem;
+    Axis<T> ax{};
+    // boundary
+    DevMem twx, twy, Wl, Wr, Wf, Wb, Gx, Gy, rows, FT, VX, VY, Zs;
+    DevMem bxc_II, bxr_a, bxr_b, byc_II, byr_a, byr_b, bxc_l, bxr_l, byc_l, byr_l;
+    BoundaryDev<T> bd{};
+    // step tables
+    DevMem steps, acts, gate_base;
+    // transmitter dependent
+    DevMem src_coef, rx_base, rx_comp, rx_w, ef0, efs, e_l1, b_l1;
+    SourceTable<T> src{};
+    RxDev<T> rd{};
+    int cur = 0;  // buffer holding the current state
+    // graph cache
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // indexed by the starting buffer
+    int gsteps = 0;
+
+    ~SimImpl() override {
+        for (auto &e : gexec) if (e) cudaGraphExecDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    FieldSet<T> fs(int b) {
+        return {fld[b][0].as<T>(), fld[b][1].as<T>(), fld[b][2].as<T>(), fld[b][3].as<T>(), fld[b][4].as<T>(),
+                fld[b][5].as<T>()};
+    }
+
+    template <class U> void upload(DevMem &m, const std::vector<U> &v) {
+        m.alloc(v.size() * sizeof(U));
+        dev_bytes += m.n;
+        if (!v.empty()) CK(cudaMemcpy(m.p, v.data(), m.n, cudaMemcpyHostToDevice));
+    }
+    template <class U> std::vector<T> conv(const std::vector<U> &v) { return std::vector<T>(v.begin(), v.end()); }
+
+    void init() override {
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        const Model &m = model;
+        g = make_geom(m.L, m.M, m.N);
+        const size_t vol = (size_t)g.total() * sizeof(T);
+        for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 6; c++) {
+                fld[b][c].alloc(vol);
+                dev_bytes += vol;
+                CK(cudaMemsetAsync(fld[b][c].p, 0, vol, stream));
+            }
+        {  // conductivity in the padded layout, plane -1 (air) and padding zero
+            std::vector<T> h((size_t)g.total(), T(0));
+            for (int k = 0; k < m.N; k++)
+                for (int j = 0; j < m.M; j++)
+                    for (int i = 0; i < m.L; i++) h[g.at(i, j, k)] = (T)m.in.con[((size_t)k * m.M + j) * m.L + i];
+            upload(con, h);
+        }
+        {  // axis tables
+            std::vector<T> t;
+            auto put = [&](const std::vector<double> &v) { size_t o = t.size(); for (double x : v) t.push_back((T)x); return o; };
+            std::vector<double> rdx(m.L), rdy(m.M), rdz(m.N), rdx2(m.L, 0), rdy2(m.M, 0), rdzs(m.N);
+            for (int i = 0; i < m.L; i++) { rdx[i] = 1.0 / m.dxk[i]; if (i) rdx2[i] = 1.0 / (m.dxk[i - 1] + m.dxk[i]); }
+            for (int j = 0; j < m.M; j++) { rdy[j] = 1.0 / m.dyk[j]; if (j) rdy2[j] = 1.0 / (m.dyk[j - 1] + m.dyk[j]); }
+            for (int k = 0; k < m.N; k++) { rdz[k] = 1.0 / m.dzk[k]; rdzs[k] = k ? 1.0 / (m.dzk[k] + m.dzk[k - 1]) : 1.0 / (2.0 * m.dzk[0]); }
+            size_t o[9];
+            o[0] = put(m.dxk); o[1] = put(m.dyk); o[2] = put(m.dzk); o[3] = put(rdx); o[4] = put(rdy); o[5] = put(rdz);
+            o[6] = put(rdx2); o[7] = put(rdy2); o[8] = put(rdzs);
+            upload(axis_mem, t);
+            const T *b = axis_mem.as<T>();
+            ax = {b + o[0], b + o[1], b + o[2], b + o[3], b + o[4], b + o[5], b + o[6], b + o[7], b + o[8]};
+        }
+        init_boundary();
+        init_steps();
+        CK(cudaStreamSynchronize(stream));
+    }
+
+    void init_boundary() {
+        const Model &m = model;
+        const int L1 = m.L1, M1 = m.M1, H = L1 / 2 + 1;
+        auto tw = [&](int n, DevMem &d) {
+            std::vector<C2<T>> h(n);
+            for (int k = 0; k < n; k++) {
+                double a = -2.0 * kPi * (double)k / (double)n;
+                h[k] = {(T)std::cos(a), (T)std::sin(a)};
+            }
+            upload(d, h);
+        };
+        tw(L1, twx);
+        tw(M1, twy);
+        upload(Wl, conv(m.Wl)); upload(Wr, conv(m.Wr)); upload(Wf, conv(m.Wf)); upload(Wb, conv(m.Wb));
+        // continuation filters of FBz_to_FBxFBy (UpContinuation_gpu.cu:113-164) as i*g; the two
+        // self-conjugate columns keep their Hermitian part so the inverse transform is real
+        std::vector<double> gx((size_t)H * M1), gy((size_t)H * M1);
+        const double dxm = m.in.dxmin, dym = m.in.dymin, dzm = m.in.dzmin;
+        for (int kx = 0; kx < H; kx++)
+            for (int ky = 0; ky < M1; ky++) {
+                double v1 = ky < M1 / 2 + 1 ? (1.0 * kPi * ky) / M1 * (dzm / dym) : -(1.0 * kPi * (M1 - ky)) / M1 * (dzm / dym);
+                double u1 = (1.0 * kPi * kx) / L1 * (dzm / dxm);
+                double a, b;
+                if (kx == 0 && ky == 0) { a = 1.0; b = 1.0; }
+                else {
+                    double w = std::sqrt(u1 * u1 + v1 * v1);
+                    double upcc = std::exp(-w) * (1.0 / w);
+                    a = (dxm / dym) * u1 * upcc;
+                    b = (dym / dxm) * v1 * upcc;
+                }
+                gx[(size_t)kx * M1 + ky] = a;
+                gy[(size_t)kx * M1 + ky] = b;
+            }
+        for (int kx = 0; kx < H; kx++) {
+            if (!(kx == 0 || 2 * kx == L1)) continue;
+            std::vector<double> ox(gx.begin() + (size_t)kx * M1, gx.begin() + (size_t)(kx + 1) * M1);
+            std::vector<double> oy(gy.begin() + (size_t)kx * M1, gy.begin() + (size_t)(kx + 1) * M1);
+            for (int ky = 0; ky < M1; ky++) {
+                int mk = (M1 - ky) % M1;
+                gx[(size_t)kx * M1 + ky] = 0.5 * (ox[ky] - ox[mk]);
+                gy[(size_t)kx * M1 + ky] = 0.5 * (oy[ky] - oy[mk]);
+            }
+        }
+        upload(Gx, conv(gx));
+        upload(Gy, conv(gy));
+        // rows of the uniform plane that the bilinear remap reads, and its tables
+        auto clampi = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi); };
+        std::vector<int> need;
+        for (int j = 0; j < m.M; j++) { int J = clampi(m.yBzold2New[j], 1, M1 - 1); need.push_back(J - 1); need.push_back(J); }
+        for (int j = 0; j <= m.M; j++) { int J = clampi(m.yoldBy2NewBz[j], 1, M1 - 1); need.push_back(J - 1); need.push_back(J); }
+        std::sort(need.begin(), need.end());
+        need.erase(std::unique(need.begin(), need.end()), need.end());
+        std::vector<int> slot(M1, -1);
+        for (size_t s = 0; s < need.size(); s++) slot[need[s]] = (int)s;
+        upload(rows, need);
+        std::vector<int> hbxcII(m.L + 1), hbxra(m.M), hbxrb(m.M), hbycII(m.L), hbyra(m.M + 1), hbyrb(m.M + 1);
+        std::vector<double> hbxcl(m.L + 1), hbxrl(m.M), hbycl(m.L), hbyrl(m.M + 1);
+        for (int i = 0; i <= m.L; i++) {
+            int II = clampi(m.xoldBx2NewBz[i], 1, L1 - 1);
+            double Xp = i == m.L ? m.X[m.L - 1] + 0.5 * m.dx[m.L - 1] : m.X[i] - 0.5 * m.dx[i];
+            hbxcII[i] = II;
+            hbxcl[i] = (Xp - m.Xn[II - 1]) / (m.Xn[II] - m.Xn[II - 1]);
+        }
+        for (int j = 0; j < m.M; j++) {
+            int J = clampi(m.yBzold2New[j], 1, M1 - 1);
+            hbxra[j] = slot[J - 1]; hbxrb[j] = slot[J];
+            hbxrl[j] = (m.Y[j] - m.Yn[J - 1]) / (m.Yn[J] - m.Yn[J - 1]);
+        }
+        for (int i = 0; i < m.L; i++) {
+            int II = clampi(m.xBzold2New[i], 1, L1 - 1);
+            hbycII[i] = II;
+            hbycl[i] = (m.X[i] - m.Xn[II - 1]) / (m.Xn[II] - m.Xn[II - 1]);
+        }
+        for (int j = 0; j <= m.M; j++) {
+            int J = clampi(m.yoldBy2NewBz[j], 1, M1 - 1);
+            double Yp = j == m.M ? m.Y[m.M - 1] + 0.5 * m.dy[m.M - 1] : m.Y[j] - 0.5 * m.dy[j];
+            hbyra[j] = slot[J - 1]; hbyrb[j] = slot[J];
+            hbyrl[j] = (Yp - m.Yn[J - 1]) / (m.Yn[J] - m.Yn[J - 1]);
+        }
+        upload(bxc_II, hbxcII); upload(bxr_a, hbxra); upload(bxr_b, hbxrb);
+        upload(byc_II, hbycII); upload(byr_a, hbyra); upload(byr_b, hbyrb);
+        upload(bxc_l, conv(hbxcl)); upload(bxr_l, conv(hbxrl)); upload(byc_l, conv(hbycl)); upload(byr_l, conv(hbyrl));
+        const int S = (int)need.size();
+        FT.alloc((size_t)m.M * H * sizeof(C2<T>)); dev_bytes += FT.n;
+        VX.alloc((size_t)S * H * sizeof(C2<T>)); dev_bytes += VX.n;
+        VY.alloc((size_t)S * H * sizeof(C2<T>)); dev_bytes += VY.n;
+        Zs.alloc((size_t)S * L1 * sizeof(C2<T>)); dev_bytes += Zs.n;
+        BoundaryDev<T> &B = bd;
+        B.L1 = L1; B.M1 = M1; B.H = H; B.M = m.M;
+        B.AnLx = m.AnLx_New; B.Nx = m.in.Nx; B.AL = m.in.ALx1 + m.in.ALx2; B.ox = m.ox; B.n1 = m.n1; B.n2 = m.n2;
+        B.Any = m.Any_New; B.Ny = m.in.Ny; B.Ay = m.in.Ay1 + m.in.Ay2; B.oy = m.oy; B.n3 = m.n3;
+        B.px = make_plan(L1); B.py = make_plan(M1);
+        B.twx = twx.as<C2<T>>(); B.twy = twy.as<C2<T>>();
+        B.Wl = Wl.as<T>(); B.Wr = Wr.as<T>(); B.Wf = Wf.as<T>(); B.Wb = Wb.as<T>();
+        B.Gx = Gx.as<T>(); B.Gy = Gy.as<T>();
+        B.S = S; B.rows = rows.as<int>();
+        B.FT = FT.as<C2<T>>(); B.VX = VX.as<C2<T>>(); B.VY = VY.as<C2<T>>(); B.Z = Zs.as<C2<T>>();
+        B.bxc_II = bxc_II.as<int>(); B.bxr_a = bxr_a.as<int>(); B.bxr_b = bxr_b.as<int>();
+        B.byc_II = byc_II.as<int>(); B.byr_a = byr_a.as<int>(); B.byr_b = byr_b.as<int>();
+        B.bxc_l = bxc_l.as<T>(); B.bxr_l = bxr_l.as<T>(); B.byc_l = byc_l.as<T>(); B.byr_l = byr_l.as<T>();
+        B.inv_norm = (T)(1.0 / (double)(L1 * M1));
+        size_t need_smem = boundary_smem_need(B, m.L);
+        int maxsm = 0;
+        CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        if (need_smem > (size_t)maxsm)
+            throw Error(TCSEM_ERR_INVALID, "continuation plane too large for the shared-memory FFT (" +
+                                               std::to_string(L1) + " x " + std::to_string(M1) + ")");
+        CK(boundary_configure(B, m.L));
+    }
+
+    void init_steps() {
+        const Schedule &S = sched;
+        std::vector<StepScalars<T>> st(S.nsteps);
+        std::vector<StepEntryActs> ac(S.nsteps);
+        for (long n = 0; n < S.nsteps; n++) {
+            st[n].lam2 = (T)(2.0 * S.lam[n]);
+            st[n].dt = (T)S.dt1[n];
+            st[n].c4 = (T)(4.0 * S.dt1[n] / model.mu0);
+            st[n].dtb = (T)S.dtB[n];
+            st[n].wave = (T)S.wave[n];
+            const StepActions &a = S.act[n];
+            ac[n] = {a.e_slot, a.e_first, a.e_count, a.b_slot, a.b_first, a.b_count};
+        }
+        upload(steps, st);
+        upload(acts, ac);
+        upload(e_l1, conv(S.e_l1));
+        upload(b_l1, conv(S.b_l1));
+        gate_base.alloc(sizeof(int));
+        dev_bytes += sizeof(int);
+        gsteps = opts.graph_steps > 0 ? opts.graph_steps : 64;
+        if (gsteps % 2) gsteps++;
+    }
+
+    void select(int t) override {
+        if (t < 0 || t >= (int)model.in.tx.size()) throw Error(TCSEM_ERR_INVALID, "transmitter index out of range");
+        if (t == itx) return;
+        const Model &m = model;
+        // sources
+        std::vector<SourceSegment> segs = m.sources(t, opts.fix_dual_bipole != 0);
+        if ((int)segs.size() > kMaxSeg) throw Error(TCSEM_ERR_INVALID, "too many source segments");
+        std::vector<T> coef;
+        src = SourceTable<T>{};
+        src.nseg = (int)segs.size();
+        for (int q = 0; q < src.nseg; q++) {
+            const SourceSegment &s = segs[q];
+            src.comp[q] = s.comp; src.i[q] = s.i; src.j[q] = s.j; src.k[q] = s.k; src.count[q] = s.count;
+            src.off[q] = (int)coef.size();
+            for (double c : s.coef) coef.push_back((T)(s.gain * c));
+        }
+        upload(src_coef, coef);
+        src.coef = src_coef.as<T>();
+        // receivers
+        std::vector<RxStencil> sts = m.rx_stencils(t);
+        const int nr = m.in.tx[t].nr;
+        std::vector<long long> base(sts.size());
+        std::vector<int> comp(sts.size());
+        std::vector<T> w(sts.size() * 12);
+        for (size_t q = 0; q < sts.size(); q++) {
+            base[q] = g.at(sts[q].s1, sts[q].s2, sts[q].s3);
+            comp[q] = sts[q].comp;
+            for (int a = 0; a < 4; a++) { w[q * 12 + a] = (T)sts[q].wx[a]; w[q * 12 + 4 + a] = (T)sts[q].wy[a]; w[q * 12 + 8 + a] = (T)sts[q].wz[a]; }
+        }
+        upload(rx_base, base); upload(rx_comp, comp); upload(rx_w, w);
+        ef0.alloc((size_t)2 * m.NComp * nr * sizeof(T));
+        efs.alloc((size_t)nr * m.NComp * m.in.Nt * sizeof(T));
+        rd.nr = nr; rd.NComp = m.NComp; rd.nefcmp = m.nefcmp; rd.Nt = m.in.Nt;
+        rd.base = rx_base.as<long long>(); rd.comp = rx_comp.as<int>(); rd.w = rx_w.as<T>();
+        rd.ef0 = ef0.as<T>(); rd.efs = efs.as<T>(); rd.e_l1 = e_l1.as<T>(); rd.b_l1 = b_l1.as<T>();
+        rd.acts = acts.as<StepEntryActs>();
+        itx = t;
+        for (auto &e : gexec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+    }
+
+    void zero_state() {
+        for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 6; c++) CK(cudaMemsetAsync(fld[b][c].p, 0, fld[b][c].n, stream));
+        if (ef0.n) CK(cudaMemsetAsync(ef0.p, 0, ef0.n, stream));
+        if (efs.n) CK(cudaMemsetAsync(efs.p, 0, efs.n, stream));
+        CK(cudaMemsetAsync(gate_base.p, 0, sizeof(int), stream));
+        cur = 0;
+        step = 0;
+    }
+
+    void begin(int t) override {
+        select(t);
+        zero_state();
+        begun = true;
+    }
+
+    // one step of main.cu:219-273 on the buffers starting at `b`
+    void enqueue_step(int b, StepGate gate) {
+        FieldSet<T> in = fs(b), out = fs(b ^ 1);
+        launch_boundary<T>(bd, g, in.bz, in.bx, in.by, gate, stream);
+        launch_fused_sweep<T>(g, in, out, con.as<T>(), ax, StepScalars<T>{}, steps.as<StepScalars<T>>(), gate, src,
+                              stream);
+        launch_rx<T>(rd, out, g, gate, RxAction{-1, 0, 0, -1, 0, 0}, stream);
+    }
+
+    cudaGraphExec_t graph_for(int b) {
+        if (gexec[b]) return gexec[b];
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int s = 0; s < gsteps; s++) enqueue_step(b ^ (s & 1), StepGate{gate_base.as<int>(), s, sched.nsteps});
+        launch_advance(gate_base.as<int>(), gsteps, stream);
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&gexec[b], graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        return gexec[b];
+    }
+
+    void advance(long n, int *done) override {
+        if (!begun) throw Error(TCSEM_ERR_STATE, "tcsem_begin must precede tcsem_advance");
+        long todo = std::min(sched.nsteps - step, std::max(0L, n));
+        // whole captured blocks (an even number of steps returns the state to `cur`)
+        while (todo >= gsteps) {
+            CK(cudaGraphLaunch(graph_for(cur), stream));
+            step += gsteps;
+            todo -= gsteps;
+        }
+        // remainder: the same kernels launched one by one, gated on the same counter
+        if (todo > 0) {
+            for (long q = 0; q < todo; q++)
+                enqueue_step(cur ^ (int)(q & 1), StepGate{gate_base.as<int>(), (int)q, sched.nsteps});
+            launch_advance(gate_base.as<int>(), (int)todo, stream);
+            if (todo & 1) cur ^= 1;
+            step += todo;
+        }
+        CK(cudaGetLastError());
+        if (done) *done = step >= sched.nsteps;
+    }
+
+    void traces(double *out) override {
+        CK(cudaStreamSynchronize(stream));
+        std::vector<T> h(efs.n / sizeof(T));
+        CK(cudaMemcpy(h.data(), efs.p, efs.n, cudaMemcpyDeviceToHost));
+        bool finite = true;
+        for (size_t q = 0; q < h.size(); q++) { out[q] = (double)h[q]; finite &= std::isfinite(out[q]); }
+        if (!finite) throw Error(TCSEM_ERR_NUMERIC, "non-finite receiver samples");
+    }
+
+    // ---- per-stage seam
+    void upcontinuation() override {
+        FieldSet<T> f = fs(cur);
+        launch_boundary<T>(bd, g, f.bz, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+        CK(cudaGetLastError());
+    }
+    StepScalars<T> scal(double lam, double dt, double dtb, double wave) {
+        StepScalars<T> s;
+        s.lam2 = (T)(2.0 * lam); s.dt = (T)dt; s.c4 = (T)(4.0 * dt / model.mu0); s.dtb = (T)dtb; s.wave = (T)wave;
+        return s;
+    }
+    void need_tx() { if (itx < 0) select(0); }
+    void electric_field(double lam, double dt, double wave) override {
+        need_tx();
+        launch_update_e<T>(g, fs(cur), con.as<T>(), ax, scal(lam, dt, 0, wave), src, stream);
+        CK(cudaGetLastError());
+    }
+    void bderivate(double dtb) override {
+        launch_bderivate<T>(g, fs(cur), ax, (T)dtb, stream);
+        CK(cudaGetLastError());
+    }
+    void fused_step(double lam, double dt, double dtb, double wave) override {
+        need_tx();
+        // the sweep writes every updated cell of the other buffer; the air plane must follow the state
+        T *dst_bx = fs(cur ^ 1).bx, *dst_by = fs(cur ^ 1).by;
+        launch_fused_sweep<T>(g, fs(cur), fs(cur ^ 1), con.as<T>(), ax, scal(lam, dt, dtb, wave), nullptr,
+                              StepGate{nullptr, 0, 0}, src, stream);
+        CK(cudaMemcpyAsync(dst_bx, fs(cur).bx, g.PS * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(dst_by, fs(cur).by, g.PS * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaGetLastError());
+        cur ^= 1;
+    }
+    void rx_sample(int efield, int slot, double *values) override {
+        need_tx();
+        if (slot < 0 || slot > 1) throw Error(TCSEM_ERR_INVALID, "slot must be 0 or 1");
+        RxAction a{-1, 0, 0, -1, 0, 0};
+        if (efield) a.e_slot = slot; else a.b_slot = slot;
+        launch_rx<T>(rd, fs(cur), g, StepGate{nullptr, 0, 0}, a, stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(stream));
+        size_t n = (size_t)model.NComp * rd.nr;
+        std::vector<T> h(n);
+        CK(cudaMemcpy(h.data(), ef0.as<T>() + (size_t)slot * n, n * sizeof(T), cudaMemcpyDeviceToHost));
+        for (size_t q = 0; q < n; q++) values[q] = (double)h[q];
+    }
+
+    // ---- field access in the reference layout
+    DevMem &field_mem(int comp, int b) {
+        if (comp == TCSEM_CON) return con;
+        if (comp == TCSEM_BXAIR) return fld[b][3];
+        if (comp == TCSEM_BYAIR) return fld[b][4];
+        return fld[b][comp];
+    }
+    void get_field(int comp, double *h) override {
+        int nx, ny, nz, z0;
+        extents(comp, nx, ny, nz, z0);
+        CK(cudaStreamSynchronize(stream));
+        DevMem &dm = field_mem(comp, cur);
+        std::vector<T> buf((size_t)g.total());
+        CK(cudaMemcpy(buf.data(), dm.p, buf.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        size_t q = 0;
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) h[q++] = (double)buf[g.at(i, j, k + z0)];
+    }
+    void set_field(int comp, const double *h) override {
+        int nx, ny, nz, z0;
+        extents(comp, nx, ny, nz, z0);
+        CK(cudaStreamSynchronize(stream));
+        DevMem &dm = field_mem(comp, cur);
+        std::vector<T> buf((size_t)g.total());
+        CK(cudaMemcpy(buf.data(), dm.p, buf.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        size_t q = 0;
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) buf[g.at(i, j, k + z0)] = (T)h[q++];
+        CK(cudaMemcpy(dm.p, buf.data(), buf.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (comp != TCSEM_CON) {  // keep the other buffer consistent for the fused sweep's untouched cells
+            DevMem &other = field_mem(comp, cur ^ 1);
+            CK(cudaMemcpy(other.p, buf.data(), buf.size() * sizeof(T), cudaMemcpyHostToDevice));
+        }
+    }
+
+    void timed_advance(long n, double *ms_out) override {
+        if (!begun) throw Error(TCSEM_ERR_STATE, "tcsem_begin must precede tcsem_timed_advance");
+        graph_for(cur);  // capture (once) outside the timed region
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaStreamSynchronize(stream));
+        CK(cudaEventRecord(e0, stream));
+        advance(n, nullptr);
+        CK(cudaEventRecord(e1, stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (ms_out) *ms_out = ms;
+    }
+
+    void time_steps(int t, long n, double *tot, double *sweep, double *bnd) override {
+        begin(t);
+        n = std::min(n, sched.nsteps);
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        graph_for(cur);  // capture outside the timed region
+        graph_for(cur ^ 1);
+        CK(cudaStreamSynchronize(stream));
+        CK(cudaEventRecord(e0, stream));
+        advance(n, nullptr);
+        CK(cudaEventRecord(e1, stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (tot) *tot = ms;
+        const int reps = 20;
+        if (sweep) {
+            StepScalars<T> s = scal(sched.lam[0], sched.dt1[0], sched.dtB[0], 0.0);
+            CK(cudaEventRecord(e0, stream));
+            for (int r = 0; r < reps; r++)
+                launch_fused_sweep<T>(g, fs(r & 1), fs((r & 1) ^ 1), con.as<T>(), ax, s, nullptr, StepGate{nullptr, 0, 0},
+                                      src, stream);
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            *sweep = ms / reps;
+        }
+        if (bnd) {
+            CK(cudaEventRecord(e0, stream));
+            for (int r = 0; r < reps; r++) {
+                FieldSet<T> f = fs(r & 1);
+                launch_boundary<T>(bd, g, f.bz, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+            }
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            *bnd = ms / reps;
+        }
+        CK(cudaGetLastError());
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        begun = false;
+    }
+};
+
+}  // namespace tcsem
+
+// ================================================================== C ABI
+using namespace tcsem;
+
+struct tcsem_sim {
+    std::unique_ptr<SimBase> impl;
+};
+
+static thread_local std::string g_open_err;
+
+template <class F> static tcsem_status guard(tcsem_sim_t *s, F &&f) {
+    if (!s || !s->impl) return TCSEM_ERR_INVALID;
+    try {
+        CK(cudaSetDevice(s->impl->device));
+        f(*s->impl);
+        return TCSEM_OK;
+    } catch (const Error &e) {
+        s->impl->err = e.what();
+        return (tcsem_status)e.code;
+    } catch (const std::bad_alloc &) {
+        s->impl->err = "host allocation failed";
+        return TCSEM_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        s->impl->err = e.what();
+        return TCSEM_ERR_INVALID;
+    }
+}
+
+extern "C" {
+
+void tcsem_default_opts(tcsem_opts *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->precision = TCSEM_FP32;
+}
+
+tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t **out) {
+    if (!dir || !out) { g_open_err = "null argument"; return TCSEM_ERR_INVALID; }
+    *out = nullptr;
+    tcsem_opts o;
+    tcsem_default_opts(&o);
+    if (opts) o = *opts;
+    if (o.precision == 0) o.precision = TCSEM_FP32;
+    if (o.precision != TCSEM_FP32 && o.precision != TCSEM_FP64) { g_open_err = "precision must be 32 or 64"; return TCSEM_ERR_INVALID; }
+    try {
+        std::unique_ptr<SimBase> impl;
+        if (o.precision == TCSEM_FP64) impl.reset(new SimImpl<double>());
+        else impl.reset(new SimImpl<float>());
+        impl->opts = o;
+        impl->device = o.device;
+        impl->model.build(read_survey_dir(dir));
+        impl->sched = impl->model.schedule();
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device || o.device < 0)
+            throw Error(TCSEM_ERR_CUDA, "no usable CUDA device");
+        impl->init();
+        tcsem_sim_t *s = new tcsem_sim;
+        s->impl = std::move(impl);
+        *out = s;
+        return TCSEM_OK;
+    } catch (const Error &e) {
+        g_open_err = e.what();
+        return (tcsem_status)e.code;
+    } catch (const std::bad_alloc &) {
+        g_open_err = "host allocation failed";
+        return TCSEM_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        g_open_err = e.what();
+        return TCSEM_ERR_INVALID;
+    }
+}
+
+const char *tcsem_open_error(void) { return g_open_err.c_str(); }
+
+tcsem_status tcsem_close(tcsem_sim_t *s) {
+    if (!s) return TCSEM_ERR_INVALID;
+    if (s->impl) cudaSetDevice(s->impl->device);
+    delete s;
+    return TCSEM_OK;
+}
+
+const char *tcsem_last_error(const tcsem_sim_t *s) { return s && s->impl ? s->impl->err.c_str() : "invalid handle"; }
+
+tcsem_status tcsem_get_info(const tcsem_sim_t *s, tcsem_info *o) {
+    if (!s || !s->impl || !o) return TCSEM_ERR_INVALID;
+    const SimBase &b = *s->impl;
+    const Model &m = b.model;
+    o->L = m.L; o->M = m.M; o->N = m.N; o->L1 = m.L1; o->M1 = m.M1;
+    o->NRx = (int)m.in.rx.size(); o->NTx = (int)m.in.tx.size(); o->Nt = m.in.Nt; o->NComp = m.NComp; o->nefcmp = m.nefcmp;
+    o->nsteps = b.sched.nsteps;
+    o->precision = b.opts.precision;
+    o->device_bytes = b.dev_bytes;
+    return TCSEM_OK;
+}
+
+tcsem_status tcsem_begin(tcsem_sim_t *s, int itx) { return guard(s, [&](SimBase &b) { b.begin(itx); }); }
+tcsem_status tcsem_advance(tcsem_sim_t *s, long n, int *done) { return guard(s, [&](SimBase &b) { b.advance(n, done); }); }
+tcsem_status tcsem_get_traces(tcsem_sim_t *s, double *t) {
+    return guard(s, [&](SimBase &b) {
+        if (!t) throw Error(TCSEM_ERR_INVALID, "null trace buffer");
+        if (b.itx < 0) throw Error(TCSEM_ERR_STATE, "no transmitter selected");
+        b.traces(t);
+    });
+}
+tcsem_status tcsem_synchronize(tcsem_sim_t *s) {
+    return guard(s, [&](SimBase &b) { CK(cudaStreamSynchronize(b.stream)); });
+}
+tcsem_status tcsem_run(tcsem_sim_t *s, int itx, double *t) {
+    return guard(s, [&](SimBase &b) {
+        if (!t) throw Error(TCSEM_ERR_INVALID, "null trace buffer");
+        b.begin(itx);
+        int done = 0;
+        b.advance(b.sched.nsteps, &done);
+        b.traces(t);
+    });
+}
+
+tcsem_status tcsem_write_bout(tcsem_sim_t *s, int itx, const double *t, const char *path) {
+    return guard(s, [&](SimBase &b) {
+        if (!t || !path) throw Error(TCSEM_ERR_INVALID, "null argument");
+        if (itx < 0 || itx >= (int)b.model.in.tx.size()) throw Error(TCSEM_ERR_INVALID, "transmitter index out of range");
+        // main.cu:280-292: int32 nr, NComp, Nt then float64 [nr][NComp][Nt]
+        int hdr[3] = {b.model.in.tx[itx].nr, b.model.NComp, b.model.in.Nt};
+        FILE *f = std::fopen(path, "wb");
+        if (!f) throw Error(TCSEM_ERR_IO, std::string("cannot write ") + path);
+        size_t n = (size_t)hdr[0] * hdr[1] * hdr[2];
+        bool ok = std::fwrite(hdr, sizeof(int), 3, f) == 3 && std::fwrite(t, sizeof(double), n, f) == n;
+        ok &= std::fclose(f) == 0;
+        if (!ok) throw Error(TCSEM_ERR_IO, std::string("short write to ") + path);
+    });
+}
+
+tcsem_status tcsem_select_tx(tcsem_sim_t *s, int itx) { return guard(s, [&](SimBase &b) { b.select(itx); }); }
+tcsem_status tcsem_upcontinuation(tcsem_sim_t *s) { return guard(s, [&](SimBase &b) { b.upcontinuation(); }); }
+tcsem_status tcsem_electric_field(tcsem_sim_t *s, double lam, double dt, double wave) {
+    return guard(s, [&](SimBase &b) { b.electric_field(lam, dt, wave); });
+}
+tcsem_status tcsem_bderivate(tcsem_sim_t *s, double dt) { return guard(s, [&](SimBase &b) { b.bderivate(dt); }); }
+tcsem_status tcsem_fused_step(tcsem_sim_t *s, double lam, double dt, double dtb, double wave) {
+    return guard(s, [&](SimBase &b) { b.fused_step(lam, dt, dtb, wave); });
+}
+tcsem_status tcsem_rx_sample(tcsem_sim_t *s, int efield, int slot, double *v) {
+    return guard(s, [&](SimBase &b) {
+        if (!v) throw Error(TCSEM_ERR_INVALID, "null output");
+        b.rx_sample(efield, slot, v);
+    });
+}
+tcsem_status tcsem_get_field(tcsem_sim_t *s, int comp, double *h) {
+    return guard(s, [&](SimBase &b) {
+        if (!h) throw Error(TCSEM_ERR_INVALID, "null output");
+        b.get_field(comp, h);
+    });
+}
+tcsem_status tcsem_set_field(tcsem_sim_t *s, int comp, const double *h) {
+    return guard(s, [&](SimBase &b) {
+        if (!h) throw Error(TCSEM_ERR_INVALID, "null input");
+        b.set_field(comp, h);
+    });
+}
+tcsem_status tcsem_field_size(const tcsem_sim_t *s, int comp, size_t *n) {
+    if (!s || !s->impl || !n) return TCSEM_ERR_INVALID;
+    try {
+        *n = s->impl->field_count(comp);
+    } catch (const Error &e) {
+        return (tcsem_status)e.code;
+    }
+    return TCSEM_OK;
+}
+tcsem_status tcsem_get_schedule(const tcsem_sim_t *s, double *dt1, double *dt2, double *lam, double *wave, long cap) {
+    if (!s || !s->impl) return TCSEM_ERR_INVALID;
+    const Schedule &S = s->impl->sched;
+    long n = std::min(cap, S.nsteps);
+    for (long q = 0; q < n; q++) {
+        if (dt1) dt1[q] = S.dt1[q];
+        if (dt2) dt2[q] = S.dt2[q];
+        if (lam) lam[q] = S.lam[q];
+        if (wave) wave[q] = S.wave[q];
+    }
+    return TCSEM_OK;
+}
+tcsem_status tcsem_get_waveform(const tcsem_sim_t *s, int *nsrc, double *t, double *dt, double *wave) {
+    if (!s || !s->impl) return TCSEM_ERR_INVALID;
+    const Model &m = s->impl->model;
+    if (nsrc) *nsrc = m.nsrc;
+    size_t n = 2 * (size_t)m.nsrc + 1;
+    if (t) std::memcpy(t, m.tw.data(), n * sizeof(double));
+    if (dt) std::memcpy(dt, m.dtw.data(), n * sizeof(double));
+    if (wave) std::memcpy(wave, m.wave.data(), n * sizeof(double));
+    return TCSEM_OK;
+}
+tcsem_status tcsem_timed_advance(tcsem_sim_t *s, long n, double *ms) {
+    return guard(s, [&](SimBase &b) { b.timed_advance(n, ms); });
+}
+tcsem_status tcsem_time_steps(tcsem_sim_t *s, int itx, long n, double *tot, double *sw, double *bn) {
+    return guard(s, [&](SimBase &b) { b.time_steps(itx, n, tot, sw, bn); });
+}
+
+}  // extern "C"

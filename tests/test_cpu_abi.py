@@ -1,0 +1,76 @@
+"""CPU-side checks of the product library: it loads, exports every symbol the
+header declares, validates its inputs, and fails loudly without a GPU."""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def test_library_builds_and_exports_header_symbols():
+    from tcsem_fdtd_gb300 import build
+
+    build.build()
+    import tcsem_fdtd_gb300 as t
+
+    lib = t.library()
+    names = t.declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_opts_and_info_struct_layout_matches_header():
+    import tcsem_fdtd_gb300 as t
+    from tcsem_fdtd_gb300.api import Info, Opts
+
+    o = Opts()
+    t.library().tcsem_default_opts(C.byref(o))
+    assert o.precision == 32 and o.device == 0 and o.fix_dual_bipole == 0
+    assert C.sizeof(Opts) == 32
+
+
+def test_open_without_gpu_or_with_bad_inputs_fails_loudly(case_dir, tmp_path):
+    import tcsem_fdtd_gb300 as t
+
+    with pytest.raises(t.TcsemError):
+        t.Simulation(str(tmp_path))  # no input files
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        with pytest.raises(t.TcsemError) as e:
+            t.Simulation(case_dir("tiny"))
+        assert e.value.status == 4  # TCSEM_ERR_CUDA, never a silent CPU path
+
+
+def test_parse_errors_are_reported(tmp_path):
+    import tcsem_fdtd_gb300 as t
+    from tcsem_fdtd_gb300 import inputs
+
+    d = str(tmp_path / "bad")
+    inputs.write_case(inputs.case("tiny"), d)
+    with open(os.path.join(d, "Transmitter.in"), "w") as f:
+        f.write("1\n1 7 100.0 0.0 0.0 20.0 1 1\n")  # illegal orientation 7
+    with pytest.raises(t.TcsemError) as e:
+        t.Simulation(d)
+    assert e.value.status == 2
+    os.remove(os.path.join(d, "Cond.bin"))
+    with pytest.raises(t.TcsemError) as e:
+        t.Simulation(d)
+    assert e.value.status == 1
+
+
+def test_cli_usage_error_exit_code():
+    from tcsem_fdtd_gb300 import build
+
+    build.build()
+    r = subprocess.run([build.CLI, "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 2

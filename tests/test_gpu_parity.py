@@ -1,0 +1,223 @@
+"""CUDA path against the FP64 oracle, stage by stage and end to end.
+
+Tolerances (relative to the largest magnitude of the oracle array):
+  FP64 build mode: 1e-10 per stage, 1e-8 on receiver traces of whole runs;
+  FP32 production: 2e-5 per stage (5e-4 for the FFT boundary), and the whole-run
+  trace error is checked against 1% (the survey's bound for FP32 vs FP64).
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+STAGE_TOL = {64: 1e-10, 32: 2e-5}
+BOUNDARY_TOL = {64: 1e-10, 32: 5e-4}
+
+
+def rel(a, b):
+    s = np.abs(b).max()
+    return float(np.abs(a - b).max() / s) if s > 0 else float(np.abs(a).max())
+
+
+@pytest.fixture(scope="module")
+def built():
+    from tcsem_fdtd_gb300 import build
+    from oracle import oracle as orc
+
+    build.build()
+    orc.build()
+    return True
+
+
+def pair(case_dir, name, precision, **kw):
+    from oracle.oracle import Oracle
+    from tcsem_fdtd_gb300 import Simulation
+
+    d = case_dir(name)
+    return Simulation(d, precision=precision, **kw), Oracle(d)
+
+
+def randomize(sim, orc, seed, names=("Ex", "Ey", "Ez", "Bx", "By", "Bz", "BxAir", "ByAir")):
+    rng = np.random.default_rng(seed)
+    for n in names:
+        a = rng.standard_normal(orc.field_shape(n))
+        orc.set(n, a)
+        sim.set(n, a)
+
+
+@pytest.mark.parametrize("name", ["tiny", "small", "txvar", "cfg1"])
+def test_setup_and_schedule_match_oracle(built, case_dir, name):
+    sim, orc = pair(case_dir, name, 64)
+    i = sim.info
+    assert (i["L"], i["M"], i["N"], i["L1"], i["M1"], i["NRx"], i["NTx"], i["Nt"], i["NComp"], i["nefcmp"]) == (
+        orc.L, orc.M, orc.N, orc.L1, orc.M1, orc.NRx, orc.NTx, orc.Nt, orc.NComp, orc.nefcmp)
+    s, so = sim.schedule(), orc.schedule()
+    assert s["nsteps"] == so["nsteps"]
+    for k in ("dt1", "dt2", "lam", "wave"):
+        np.testing.assert_array_equal(s[k], so[k], err_msg=k)
+    t, dt, w = sim.waveform()
+    np.testing.assert_array_equal(t, orc.darray("tw"))
+    np.testing.assert_array_equal(dt, orc.darray("dtw")[: len(dt)])
+    np.testing.assert_array_equal(w, orc.darray("wave"))
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_electric_field_stage(built, case_dir, name, precision):
+    sim, orc = pair(case_dir, name, precision)
+    sched = orc.schedule()
+    for step in (3, 250):  # source on, source off
+        randomize(sim, orc, 100 + step)
+        lam, dt, wave = sched["lam"][step], sched["dt1"][step], sched["wave"][step]
+        sim.select_tx(0)
+        sim.electric_field(lam, dt, wave)
+        orc.electric_field(0, lam, dt, wave)
+        for n in ("Ex", "Ey", "Ez"):
+            assert rel(sim.get(n), orc.get(n)) < STAGE_TOL[precision], (n, step)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_bderivate_stage(built, case_dir, name, precision):
+    sim, orc = pair(case_dir, name, precision)
+    randomize(sim, orc, 7)
+    dtb = orc.schedule()["dt1"][300]
+    sim.bderivate(dtb)
+    orc.bderivate(dtb)
+    for n in ("Bx", "By", "Bz"):
+        assert rel(sim.get(n), orc.get(n)) < STAGE_TOL[precision], n
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("name", ["tiny", "small", "cfg1"])
+def test_upcontinuation_stage(built, case_dir, name, precision):
+    sim, orc = pair(case_dir, name, precision)
+    randomize(sim, orc, 11, names=("Bz",))
+    sim.upcontinuation()
+    orc.upcontinuation()
+    for n in ("BxAir", "ByAir"):
+        assert rel(sim.get(n), orc.get(n)) < BOUNDARY_TOL[precision], n
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("name", ["tiny", "small", "txvar"])
+def test_fused_sweep_equals_e_then_b(built, case_dir, name, precision):
+    sim, orc = pair(case_dir, name, precision)
+    sched = orc.schedule()
+    for step in (5, 260):
+        randomize(sim, orc, 31 + step)
+        lam, dt, dtb, wave = sched["lam"][step], sched["dt1"][step], 0.5 * (sched["dt1"][step] + sched["dt2"][step]), sched["wave"][step]
+        sim.select_tx(0)
+        sim.fused_step(lam, dt, dtb, wave)
+        orc.electric_field(0, lam, dt, wave)
+        orc.bderivate(dtb)
+        for n in ("Ex", "Ey", "Ez", "Bx", "By", "Bz"):
+            assert rel(sim.get(n), orc.get(n)) < STAGE_TOL[precision], (n, step)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_receiver_interpolation_stage(built, case_dir, precision):
+    sim, orc = pair(case_dir, "tiny", precision)
+    randomize(sim, orc, 5)
+    iv, _, rxn = orc.tx(0)
+    nr = int(iv[1])
+    comps = [c for c in range(6) if True]
+    for efield in (1, 0):
+        got = sim.rx_sample(efield, 0, nr)
+        exp = np.zeros_like(got)
+        pos = 0 if efield else orc.nefcmp
+        for c in (range(3) if efield else range(3, 6)):
+            exp[pos] = [orc.rx_interp(c, int(r) - 1) for r in rxn]
+            pos += 1
+        sl = slice(0, orc.nefcmp) if efield else slice(orc.nefcmp, orc.NComp)
+        assert rel(got[sl], exp[sl]) < STAGE_TOL[precision] * 10
+
+
+def trace_error(got, exp):
+    """max over traces of max|got-exp| / max|exp| (traces with zero peak skipped)."""
+    worst = 0.0
+    for r in range(exp.shape[0]):
+        for c in range(exp.shape[1]):
+            pk = np.abs(exp[r, c]).max()
+            if pk > 0:
+                worst = max(worst, np.abs(got[r, c] - exp[r, c]).max() / pk)
+    return worst
+
+
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_full_run_fp64_matches_oracle(built, case_dir, name):
+    sim, orc = pair(case_dir, name, 64)
+    exp, n = orc.run(0)
+    got = sim.run(0, nr=exp.shape[0])
+    assert n == sim.info["nsteps"]
+    assert trace_error(got, exp) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_full_run_fp32_within_one_percent(built, case_dir, name):
+    sim, orc = pair(case_dir, name, 32)
+    exp, _ = orc.run(0)
+    got = sim.run(0, nr=exp.shape[0])
+    err = trace_error(got, exp)
+    print(f"{name} fp32 trace error {err:.3e}")
+    assert err < 1e-2
+
+
+def test_all_transmitter_orientations_fp64(built, case_dir):
+    sim, orc = pair(case_dir, "txvar", 64)
+    for t in range(orc.NTx):
+        exp, _ = orc.run(t)
+        got = sim.run(t, nr=exp.shape[0])
+        assert trace_error(got, exp) < 1e-8, t
+
+
+def test_fixed_dual_bipole_option(built, case_dir):
+    sim, orc = pair(case_dir, "txvar", 64, fix_dual_bipole=True)
+    orc.set_dual_bipole_compat(False)
+    t = orc.NTx - 1  # the ort=5 transmitter
+    exp, _ = orc.run(t)
+    got = sim.run(t, nr=exp.shape[0])
+    assert trace_error(got, exp) < 1e-8
+
+
+def test_stepwise_advance_equals_run(built, case_dir):
+    sim, orc = pair(case_dir, "tiny", 32, graph_steps=16)
+    iv, _, _ = orc.tx(0)
+    nr = int(iv[1])
+    ref = sim.run(0, nr=nr)
+    sim.begin(0)
+    done = False
+    while not done:
+        done = sim.advance(16)
+    np.testing.assert_array_equal(sim.traces(nr), ref)
+
+
+def test_repeat_runs_are_bitwise_identical(built, case_dir):
+    sim, orc = pair(case_dir, "small", 32)
+    a = sim.run(0, nr=6)
+    b = sim.run(0, nr=6)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_cli_writes_reference_formats(built, case_dir, tmp_path):
+    import shutil
+
+    from tcsem_fdtd_gb300 import build
+
+    src = case_dir("tiny")
+    d = tmp_path / "run"
+    shutil.copytree(src, d)
+    r = subprocess.run([build.CLI, str(d)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = open(d / "Tx1.bout", "rb").read()
+    hdr = np.frombuffer(raw[:12], np.int32)
+    data = np.frombuffer(raw[12:], np.float64).reshape(hdr)
+    sim, orc = pair(case_dir, "tiny", 32)
+    np.testing.assert_array_equal(data, sim.run(0, nr=int(hdr[0])))
+    wf = open(d / "testwaveform.dat", "rb").read()
+    n = int(np.frombuffer(wf[:4], np.int32)[0])
+    a = np.frombuffer(wf[4:], np.float64)
+    np.testing.assert_array_equal(a[: 2 * n + 1], orc.darray("tw"))
