@@ -48,7 +48,8 @@ typedef struct {
     int device;           /* CUDA device ordinal, default 0 */
     int fix_dual_bipole;  /* 1: inject the second bipole of ort=5 at its own cells (default 0 = as the reference) */
     int graph_steps;      /* steps per captured CUDA graph, 0 = default (even numbers only) */
-    int reserved[4];
+    int zchunks;          /* z-chunks of the fused sweep, 0 = chosen from the grid and the GPU */
+    int reserved[3];
 } tcsem_opts;
 
 typedef struct {

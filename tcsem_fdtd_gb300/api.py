@@ -28,7 +28,7 @@ class TcsemError(RuntimeError):
 
 class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("fix_dual_bipole", C.c_int), ("graph_steps", C.c_int),
-                ("reserved", C.c_int * 4)]
+                ("zchunks", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class Info(C.Structure):
@@ -98,11 +98,12 @@ def _dptr(a):
 class Simulation:
     """One survey on one GPU: the handle of include/tcsem.h."""
 
-    def __init__(self, directory, precision=32, device=0, fix_dual_bipole=False, graph_steps=0):
+    def __init__(self, directory, precision=32, device=0, fix_dual_bipole=False, graph_steps=0, zchunks=0):
         L = library()
         o = Opts()
         L.tcsem_default_opts(C.byref(o))
         o.precision, o.device, o.fix_dual_bipole, o.graph_steps = precision, device, int(fix_dual_bipole), graph_steps
+        o.zchunks = zchunks
         h = C.c_void_p()
         st = L.tcsem_open_dir(os.fsencode(directory), C.byref(o), C.byref(h))
         if st != 0:

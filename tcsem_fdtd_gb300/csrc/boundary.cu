@@ -87,15 +87,21 @@ __device__ C2<T> *fft_smem(C2<T> *a, C2<T> *b, const FFTPlan &P, const C2<T> *__
 
 // ---- stage 1: x-remap of the M old rows + forward FFT along x
 template <typename T>
-__global__ void k_rows_fwd(BoundaryDev<T> bd, const T *__restrict__ bz, Geom g, StepGate gate) {
+__global__ void k_rows_fwd(BoundaryDev<T> bd, const T *__restrict__ bz, const T *__restrict__ tot, int nch, Geom g,
+                           StepGate gate) {
     if (gate.base && gate.step() >= gate.nsteps) return;
     extern __shared__ unsigned char smem_raw[];
     C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw);
     C2<T> *b = a + bd.L1;
     T *row = reinterpret_cast<T *>(b + bd.L1);
     const int j = blockIdx.x, L = g.L;
-    const T *src = bz + g.at(0, j, 0);  // plane 0 of Bz
-    for (int i = threadIdx.x; i < L; i += blockDim.x) row[i] = src[i];
+    const T *src = bz + g.at(0, j, 0);  // plane 0 of Bz (chunk-partial: add the totals of the chunks below)
+    const long long plane = (long long)(g.M + 2) * g.XP, col0 = (long long)(j + 1) * g.XP + 4;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        T v = src[i];
+        for (int c = 1; c < nch; c++) v += tot[c * plane + col0 + i];
+        row[i] = v;
+    }
     __syncthreads();
     const int anl = bd.AnLx, nx = bd.Nx, AL = bd.AL;
     for (int c = threadIdx.x; c < bd.L1; c += blockDim.x) {
@@ -244,9 +250,9 @@ template <typename T> cudaError_t boundary_configure(const BoundaryDev<T> &bd, i
 }
 
 template <typename T>
-void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, T *bx, T *by, StepGate gate,
-                     cudaStream_t st) {
-    k_rows_fwd<T><<<g.M, 256, smem_rows(bd, g.L), st>>>(bd, bz, g, gate);
+void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
+                     StepGate gate, cudaStream_t st) {
+    k_rows_fwd<T><<<g.M, 256, smem_rows(bd, g.L), st>>>(bd, bz, tot, nch, g, gate);
     k_cols<T><<<bd.H, 256, smem_cols(bd), st>>>(bd, gate);
     k_rows_inv<T><<<bd.S, 256, smem_inv(bd), st>>>(bd, gate);
     int n = (g.L + 1) * g.M + g.L * (g.M + 1);
@@ -279,7 +285,8 @@ cudaError_t launch_fft_rows(const FFTPlan &P, const void *tw, const void *in, vo
 #define INST(T)                                                                                            \
     template size_t boundary_smem_need<T>(const BoundaryDev<T> &, int);                                   \
     template cudaError_t boundary_configure<T>(const BoundaryDev<T> &, int);                              \
-    template void launch_boundary<T>(const BoundaryDev<T> &, const Geom &, const T *, T *, T *, StepGate,         \
+    template void launch_boundary<T>(const BoundaryDev<T> &, const Geom &, const T *, const T *, int, T *, T *,  \
+                                     StepGate,                                                            \
                                      cudaStream_t);                                                       \
     template cudaError_t launch_fft_rows<T>(const FFTPlan &, const void *, const void *, void *, int, int, cudaStream_t);
 INST(float)

@@ -42,8 +42,8 @@ namespace tcsem {
 template <typename T> size_t boundary_smem_need(const BoundaryDev<T> &bd, int L);
 template <typename T> cudaError_t boundary_configure(const BoundaryDev<T> &bd, int L);
 template <typename T>
-void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, T *bx, T *by, StepGate gate,
-                     cudaStream_t st);
+void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
+                     StepGate gate, cudaStream_t st);
 template <typename T>
 cudaError_t launch_fft_rows(const FFTPlan &P, const void *tw, const void *in, void *out, int rows, int inv,
                             cudaStream_t st);

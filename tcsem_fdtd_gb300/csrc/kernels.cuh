@@ -13,6 +13,7 @@
 // the air (0 S/m), and plane N of Ex/Ey/Bz is the zero bottom -- so the
 // kernels need no special case for the top or bottom plane.
 #pragma once
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -75,6 +76,13 @@ struct StepGate {
     __device__ __forceinline__ long step() const { return (long)*base + off; }
 };
 
+// z-chunks of the fused sweep: chunk c covers planes [kb[c], kb[c+1])
+constexpr int kMaxChunks = 16;
+struct ZChunks {
+    int n;
+    int kb[kMaxChunks + 1];
+};
+
 // ----------------------------------------------------------------- launchers
 // volume.cu
 template <typename T>
@@ -82,9 +90,18 @@ void launch_update_e(const Geom &g, FieldSet<T> f, const T *con, const Axis<T> &
                      const SourceTable<T> &src, cudaStream_t st);
 template <typename T>
 void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, cudaStream_t st);
+// TMA descriptors of the fused sweep's inputs: ex ey ez bx by bz of one field set, then sigma
+struct SweepMaps {
+    CUtensorMap m[7];
+};
 template <typename T>
-void launch_fused_sweep(const Geom &g, FieldSet<T> in, FieldSet<T> out, const T *con, const Axis<T> &ax,
-                        StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
-                        const SourceTable<T> &src, cudaStream_t st);
+void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
+                        const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
+                        const SourceTable<T> &src, const ZChunks &zc, int *err, cudaStream_t st);
+template <typename T> cudaError_t sweep_configure(int N);
+template <typename T> size_t sweep_smem_bytes(int N);
+int sweep_box_x();
+int sweep_box_y();
+template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, const ZChunks &zc, cudaStream_t st);
 
 }  // namespace tcsem

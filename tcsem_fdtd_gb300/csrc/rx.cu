@@ -14,19 +14,35 @@
 namespace tcsem {
 
 template <typename T>
-__device__ __forceinline__ T stencil_value(const RxDev<T> &rd, const FieldSet<T> &f, int s, const Geom &g) {
+__device__ __forceinline__ T stencil_value(const RxDev<T> &rd, const FieldSet<T> &f, int s, const Geom &g,
+                                           const T *tot, const ZChunks &zc) {
     const int comp = rd.comp[s];
     const T *F = comp == 0 ? f.ex : comp == 1 ? f.ey : comp == 2 ? f.ez : comp == 3 ? f.bx : comp == 4 ? f.by : f.bz;
     const T *w = rd.w + (size_t)s * 12;
     const long long base = rd.base[s];
     T v = T(0);
+    // chunk-partial Bz: add the totals of the chunks below each plane
+    const long long plane = (long long)(g.M + 2) * g.XP;
+    const long long col = (base % g.PS);
+    const int k3 = (int)(base / g.PS) - 1;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         T vy = T(0);
+        int cz = 0;
+        if (comp == 5 && zc.n > 1)
+            while (cz + 1 < zc.n && k3 + c >= zc.kb[cz + 1]) cz++;
 #pragma unroll
         for (int b = 0; b < 4; b++) {
             const T *row = F + base + (long long)c * g.PS + (long long)b * g.XP;
-            T vx = w[0] * row[0] + w[1] * row[1] + w[2] * row[2] + w[3] * row[3];
+            T r0 = row[0], r1 = row[1], r2 = row[2], r3 = row[3];
+            if (comp == 5 && zc.n > 1) {
+                const long long cb = col + (long long)b * g.XP;
+                for (int q = cz + 1; q < zc.n; q++) {
+                    const T *t = tot + q * plane + cb;
+                    r0 += t[0]; r1 += t[1]; r2 += t[2]; r3 += t[3];
+                }
+            }
+            T vx = w[0] * r0 + w[1] * r1 + w[2] * r2 + w[3] * r3;
             vy += w[4 + b] * vx;
         }
         v += w[8 + c] * vy;
@@ -35,7 +51,7 @@ __device__ __forceinline__ T stencil_value(const RxDev<T> &rd, const FieldSet<T>
 }
 
 template <typename T>
-__global__ void k_rx(RxDev<T> rd, FieldSet<T> f, Geom g, StepGate gate, RxAction act) {
+__global__ void k_rx(RxDev<T> rd, FieldSet<T> f, const T *tot, ZChunks zc, Geom g, StepGate gate, RxAction act) {
     if (gate.base) {
         const long st = gate.step();
         if (st >= gate.nsteps) return;
@@ -50,7 +66,7 @@ __global__ void k_rx(RxDev<T> rd, FieldSet<T> f, Geom g, StepGate gate, RxAction
     const bool efield = p < ne;
     const int slot = efield ? act.e_slot : act.b_slot;
     if (slot < 0) return;
-    const T v = stencil_value(rd, f, idx, g);
+    const T v = stencil_value(rd, f, idx, g, tot, zc);
     rd.ef0[(size_t)slot * NC * nr + idx] = v;
     const int first = efield ? act.e_first : act.b_first, count = efield ? act.e_count : act.b_count;
     const T *l1 = efield ? rd.e_l1 : rd.b_l1;
@@ -67,15 +83,18 @@ __global__ void k_advance(int *base, int by) {
 }
 
 template <typename T>
-void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const Geom &g, StepGate gate, RxAction act, cudaStream_t st) {
+void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const T *tot, const ZChunks &zc, const Geom &g, StepGate gate,
+               RxAction act, cudaStream_t st) {
     int n = rd.NComp * rd.nr;
     if (n == 0) return;
-    k_rx<T><<<(n + 127) / 128, 128, 0, st>>>(rd, f, g, gate, act);
+    k_rx<T><<<(n + 127) / 128, 128, 0, st>>>(rd, f, tot, zc, g, gate, act);
 }
 
 void launch_advance(int *base, int by, cudaStream_t st) { k_advance<float><<<1, 1, 0, st>>>(base, by); }
 
-template void launch_rx<float>(const RxDev<float> &, FieldSet<float>, const Geom &, StepGate, RxAction, cudaStream_t);
-template void launch_rx<double>(const RxDev<double> &, FieldSet<double>, const Geom &, StepGate, RxAction, cudaStream_t);
+template void launch_rx<float>(const RxDev<float> &, FieldSet<float>, const float *, const ZChunks &, const Geom &,
+                               StepGate, RxAction, cudaStream_t);
+template void launch_rx<double>(const RxDev<double> &, FieldSet<double>, const double *, const ZChunks &, const Geom &,
+                                StepGate, RxAction, cudaStream_t);
 
 }  // namespace tcsem

@@ -25,7 +25,8 @@ template <typename T> struct RxDev {
 };
 
 template <typename T>
-void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const Geom &g, StepGate gate, RxAction act, cudaStream_t st);
+void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const T *tot, const ZChunks &zc, const Geom &g, StepGate gate,
+               RxAction act, cudaStream_t st);
 void launch_advance(int *base, int by, cudaStream_t st);
 
 }  // namespace tcsem

@@ -51,6 +51,23 @@ struct DevMem {
     template <class U> U *as() const { return reinterpret_cast<U *>(p); }
 };
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link-time dependency on libcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            throw Error(TCSEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
 static FFTPlan make_plan(int n) {
     FFTPlan P{};
     P.n = n;
@@ -90,6 +107,7 @@ struct SimBase {
     virtual void set_field(int comp, const double *h) = 0;
     virtual void time_steps(int itx, long n, double *tot, double *sweep, double *bnd) = 0;
     virtual void timed_advance(long n, double *ms) = 0;
+    virtual void check_error() = 0;
     size_t field_count(int comp) const {
         size_t L = model.L, M = model.M, N = model.N;
         switch (comp) {
@@ -127,7 +145,10 @@ struct SimBase {
 // ---------------------------------------------------------------- typed impl
 template <typename T> struct SimImpl : SimBase {
     Geom g{};
-    DevMem fld[2][6], con;
+    DevMem fld[2][6], con, tot[2];  // two field sets + conductivity; per-set chunk totals of Bz
+    ZChunks zc{};
+    SweepMaps maps[2];              // TMA descriptors of each field set (+ conductivity)
+    DevMem errw;                    // device error word (a bounded wait gave up)
     DevMem axis_mem;
     Axis<T> ax{};
     // boundary
@@ -195,10 +216,68 @@ template <typename T> struct SimImpl : SimBase {
             const T *b = axis_mem.as<T>();
             ax = {b + o[0], b + o[1], b + o[2], b + o[3], b + o[4], b + o[5], b + o[6], b + o[7], b + o[8]};
         }
+        init_chunks();
+        init_maps();
         init_boundary();
         init_steps();
         CK(cudaStreamSynchronize(stream));
     }
+
+    // z-chunks of the fused sweep: enough CTAs to fill the GPU several times over
+    void init_chunks() {
+        const Model &m = model;
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        const long tiles = (long)((m.L + 63) / 64) * ((m.M + 7) / 8);  // 64 x 8 tiles of the fused sweep
+        int n = (int)std::min<long>(kMaxChunks, std::max<long>(1, (7L * sms + tiles - 1) / tiles));
+        n = std::min(n, std::max(1, m.N / 8));
+        if (opts.zchunks > 0) n = std::min(std::min(opts.zchunks, kMaxChunks), m.N);
+        zc.n = n;
+        for (int c = 0; c <= n; c++) zc.kb[c] = (int)(((long)c * m.N) / n);
+        const size_t tb = (size_t)n * g.PS * sizeof(T);
+        for (int b = 0; b < 2; b++) {
+            tot[b].alloc(tb);
+            dev_bytes += tb;
+            CK(cudaMemsetAsync(tot[b].p, 0, tb, stream));
+        }
+    }
+    void init_maps() {
+        if (g.total() >= (1LL << 31)) throw Error(TCSEM_ERR_INVALID, "grid too large for 32-bit offsets");
+        EncodeTiledFn enc = encode_tiled();
+        const cuuint64_t dims[3] = {(cuuint64_t)g.XP, (cuuint64_t)g.YP, (cuuint64_t)(g.N + 2)};
+        const cuuint64_t strides[2] = {(cuuint64_t)g.XP * sizeof(T), (cuuint64_t)g.PS * sizeof(T)};
+        const cuuint32_t box[3] = {(cuuint32_t)sweep_box_x(), (cuuint32_t)sweep_box_y(), 1};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const CUtensorMapDataType dt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        auto make = [&](void *ptr, CUtensorMap *m) {
+            CUresult r = enc(m, dt, 3, ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) throw Error(TCSEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        };
+        for (int b = 0; b < 2; b++) {
+            for (int a = 0; a < 6; a++) make(fld[b][a].p, &maps[b].m[a]);
+            make(con.p, &maps[b].m[6]);
+        }
+        errw.alloc(sizeof(int));
+        dev_bytes += sizeof(int);
+        CK(cudaMemset(errw.p, 0, sizeof(int)));
+        CK(sweep_configure<T>(g.N));
+    }
+    void check_error() override { check_device_error(); }
+    void check_device_error() {
+        int h = 0;
+        CK(cudaMemcpy(&h, errw.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) {
+            CK(cudaMemset(errw.p, 0, sizeof(int)));
+            throw Error(TCSEM_ERR_CUDA, "a bounded wait in the fused sweep gave up (copy did not arrive)");
+        }
+    }
+    void sweep(int b, StepScalars<T> s, const StepScalars<T> *table, StepGate gate) {
+        launch_fused_sweep<T>(maps[b], g, fs(b ^ 1), tot[b].as<T>(), tot[b ^ 1].as<T>(), ax, s, table, gate, src, zc,
+                              errw.as<int>(), stream);
+    }
+    void consolidate(int b) { launch_bz_consolidate<T>(g, fs(b).bz, tot[b].as<T>(), zc, stream); }
 
     void init_boundary() {
         const Model &m = model;
@@ -379,6 +458,7 @@ template <typename T> struct SimImpl : SimBase {
         if (ef0.n) CK(cudaMemsetAsync(ef0.p, 0, ef0.n, stream));
         if (efs.n) CK(cudaMemsetAsync(efs.p, 0, efs.n, stream));
         CK(cudaMemsetAsync(gate_base.p, 0, sizeof(int), stream));
+        for (int b = 0; b < 2; b++) CK(cudaMemsetAsync(tot[b].p, 0, tot[b].n, stream));
         cur = 0;
         step = 0;
     }
@@ -392,10 +472,9 @@ template <typename T> struct SimImpl : SimBase {
     // one step of main.cu:219-273 on the buffers starting at `b`
     void enqueue_step(int b, StepGate gate) {
         FieldSet<T> in = fs(b), out = fs(b ^ 1);
-        launch_boundary<T>(bd, g, in.bz, in.bx, in.by, gate, stream);
-        launch_fused_sweep<T>(g, in, out, con.as<T>(), ax, StepScalars<T>{}, steps.as<StepScalars<T>>(), gate, src,
-                              stream);
-        launch_rx<T>(rd, out, g, gate, RxAction{-1, 0, 0, -1, 0, 0}, stream);
+        launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, stream);
+        sweep(b, StepScalars<T>{}, steps.as<StepScalars<T>>(), gate);
+        launch_rx<T>(rd, out, tot[b ^ 1].as<T>(), zc, g, gate, RxAction{-1, 0, 0, -1, 0, 0}, stream);
     }
 
     cudaGraphExec_t graph_for(int b) {
@@ -435,6 +514,7 @@ template <typename T> struct SimImpl : SimBase {
 
     void traces(double *out) override {
         CK(cudaStreamSynchronize(stream));
+        check_device_error();
         std::vector<T> h(efs.n / sizeof(T));
         CK(cudaMemcpy(h.data(), efs.p, efs.n, cudaMemcpyDeviceToHost));
         bool finite = true;
@@ -445,7 +525,7 @@ template <typename T> struct SimImpl : SimBase {
     // ---- per-stage seam
     void upcontinuation() override {
         FieldSet<T> f = fs(cur);
-        launch_boundary<T>(bd, g, f.bz, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+        launch_boundary<T>(bd, g, f.bz, tot[cur].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
         CK(cudaGetLastError());
     }
     StepScalars<T> scal(double lam, double dt, double dtb, double wave) {
@@ -456,10 +536,12 @@ template <typename T> struct SimImpl : SimBase {
     void need_tx() { if (itx < 0) select(0); }
     void electric_field(double lam, double dt, double wave) override {
         need_tx();
+        consolidate(cur);
         launch_update_e<T>(g, fs(cur), con.as<T>(), ax, scal(lam, dt, 0, wave), src, stream);
         CK(cudaGetLastError());
     }
     void bderivate(double dtb) override {
+        consolidate(cur);
         launch_bderivate<T>(g, fs(cur), ax, (T)dtb, stream);
         CK(cudaGetLastError());
     }
@@ -467,8 +549,7 @@ template <typename T> struct SimImpl : SimBase {
         need_tx();
         // the sweep writes every updated cell of the other buffer; the air plane must follow the state
         T *dst_bx = fs(cur ^ 1).bx, *dst_by = fs(cur ^ 1).by;
-        launch_fused_sweep<T>(g, fs(cur), fs(cur ^ 1), con.as<T>(), ax, scal(lam, dt, dtb, wave), nullptr,
-                              StepGate{nullptr, 0, 0}, src, stream);
+        sweep(cur, scal(lam, dt, dtb, wave), nullptr, StepGate{nullptr, 0, 0});
         CK(cudaMemcpyAsync(dst_bx, fs(cur).bx, g.PS * sizeof(T), cudaMemcpyDeviceToDevice, stream));
         CK(cudaMemcpyAsync(dst_by, fs(cur).by, g.PS * sizeof(T), cudaMemcpyDeviceToDevice, stream));
         CK(cudaGetLastError());
@@ -479,7 +560,7 @@ template <typename T> struct SimImpl : SimBase {
         if (slot < 0 || slot > 1) throw Error(TCSEM_ERR_INVALID, "slot must be 0 or 1");
         RxAction a{-1, 0, 0, -1, 0, 0};
         if (efield) a.e_slot = slot; else a.b_slot = slot;
-        launch_rx<T>(rd, fs(cur), g, StepGate{nullptr, 0, 0}, a, stream);
+        launch_rx<T>(rd, fs(cur), tot[cur].as<T>(), zc, g, StepGate{nullptr, 0, 0}, a, stream);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(stream));
         size_t n = (size_t)model.NComp * rd.nr;
@@ -498,6 +579,7 @@ template <typename T> struct SimImpl : SimBase {
     void get_field(int comp, double *h) override {
         int nx, ny, nz, z0;
         extents(comp, nx, ny, nz, z0);
+        if (comp == TCSEM_BZ) consolidate(cur);
         CK(cudaStreamSynchronize(stream));
         DevMem &dm = field_mem(comp, cur);
         std::vector<T> buf((size_t)g.total());
@@ -523,6 +605,8 @@ template <typename T> struct SimImpl : SimBase {
             DevMem &other = field_mem(comp, cur ^ 1);
             CK(cudaMemcpy(other.p, buf.data(), buf.size() * sizeof(T), cudaMemcpyHostToDevice));
         }
+        if (comp == TCSEM_BZ)  // a plain Bz plane: no chunk offsets
+            for (int b = 0; b < 2; b++) CK(cudaMemset(tot[b].p, 0, tot[b].n));
     }
 
     void timed_advance(long n, double *ms_out) override {
@@ -543,7 +627,7 @@ template <typename T> struct SimImpl : SimBase {
         if (ms_out) *ms_out = ms;
     }
 
-    void time_steps(int t, long n, double *tot, double *sweep, double *bnd) override {
+    void time_steps(int t, long n, double *ms_tot, double *ms_sweep, double *bnd) override {
         begin(t);
         n = std::min(n, sched.nsteps);
         cudaEvent_t e0, e1;
@@ -558,24 +642,23 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaEventSynchronize(e1));
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, e0, e1));
-        if (tot) *tot = ms;
+        if (ms_tot) *ms_tot = ms;
         const int reps = 20;
-        if (sweep) {
+        if (ms_sweep) {
             StepScalars<T> s = scal(sched.lam[0], sched.dt1[0], sched.dtB[0], 0.0);
             CK(cudaEventRecord(e0, stream));
             for (int r = 0; r < reps; r++)
-                launch_fused_sweep<T>(g, fs(r & 1), fs((r & 1) ^ 1), con.as<T>(), ax, s, nullptr, StepGate{nullptr, 0, 0},
-                                      src, stream);
+                sweep(r & 1, s, nullptr, StepGate{nullptr, 0, 0});
             CK(cudaEventRecord(e1, stream));
             CK(cudaEventSynchronize(e1));
             CK(cudaEventElapsedTime(&ms, e0, e1));
-            *sweep = ms / reps;
+            *ms_sweep = ms / reps;
         }
         if (bnd) {
             CK(cudaEventRecord(e0, stream));
             for (int r = 0; r < reps; r++) {
                 FieldSet<T> f = fs(r & 1);
-                launch_boundary<T>(bd, g, f.bz, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+                launch_boundary<T>(bd, g, f.bz, tot[r & 1].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
             }
             CK(cudaEventRecord(e1, stream));
             CK(cudaEventSynchronize(e1));
@@ -695,7 +778,10 @@ tcsem_status tcsem_get_traces(tcsem_sim_t *s, double *t) {
     });
 }
 tcsem_status tcsem_synchronize(tcsem_sim_t *s) {
-    return guard(s, [&](SimBase &b) { CK(cudaStreamSynchronize(b.stream)); });
+    return guard(s, [&](SimBase &b) {
+        CK(cudaStreamSynchronize(b.stream));
+        b.check_error();
+    });
 }
 tcsem_status tcsem_run(tcsem_sim_t *s, int itx, double *t) {
     return guard(s, [&](SimBase &b) {

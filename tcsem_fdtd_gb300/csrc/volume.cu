@@ -5,7 +5,7 @@
 //  * reference-structured kernels (k_update_e, k_source, k_update_bxy,
 //    k_update_bz) that update one field set in place, stage by stage, as
 //    ElectricalField/Bderivate do (ElectricalFiled.cu:89-475, Bderivate.cu:79-265);
-//  * the production fused sweep (k_fused_sweep): one pass over the volume per
+//  * the production fused sweep (k_sweep): one pass over the volume per
 //    time step that reads the old E/B/sigma planes and writes the new E and B
 //    into the other buffer of a ping-pong pair.  It marches z bottom-up so the
 //    div B = 0 prefix for Bz (Bderivate.cu:202-265) runs in a register, and each
@@ -120,213 +120,447 @@ void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, cu
 }
 
 // ------------------------------------------------------------- fused sweep
+//
+// One pass per time step over the volume: old E/B/sigma planes stream into a
+// shared-memory ring through TMA bulk-tensor copies (cp.async.bulk.tensor,
+// mbarrier completion), the new E and B go to the other buffer of the
+// ping-pong pair.  Tiles are 32 x 8 columns, aligned so every TMA box starts
+// on a 16-byte boundary; one thread per column marches z bottom-up through one
+// z-chunk.  Warps 0..7 own the tile rows, warp 8 recomputes the +y halo row
+// and warp 9 the +x halo column (E and the B components the tile's Bz needs),
+// so no CTA waits for another; the -x/-y halo is plain old data in the TMA box.
+// Neighbour values of the new fields go through double-buffered shared planes
+// with one __syncthreads per z-plane:
+//   iteration k:  B(k+1)  ->  E(k)  ->  publish Ez(k), B(k+1)  ->  sync
+//                 ->  TMA of plane k-4 into the freed slot  ->  Bz(k+1)
+//
+// Bz within a chunk is the partial sum P(k) = sum_{k'=k}^{k1-1} dz div_xy B(k');
+// the true Bz(k) = P(k) + O_c with O_c = sum of the chunk totals T_c' of the
+// chunks below (c' > c).  Readers add O_c; T has one plane per chunk.
 
-namespace fs {
-constexpr int TX = 32, TY = 8;           // owned tile (x, y)
-constexpr int NT = TX * TY;              // threads per CTA
-constexpr int SX = 40, SY = TY + 2;      // shared plane: i in [i0-4, i0+36), j in [j0-1, j0+TY]
-constexpr int SP = SX * SY;
-constexpr int RW = TX + 2, RH = TY + 2;  // loaded region: i in [i0-1, i0+TX], j in [j0-1, j0+TY]
-constexpr int RN = RW * RH;              // 340 elements
-constexpr int EW = TX + 1, EH = TY + 1;  // E work region: i in [i0, i0+TX], j in [j0, j0+TY]
-constexpr int EN = EW * EH;              // 297 items
-static_assert(RN <= 2 * NT && EN <= 2 * NT, "two items per thread");
-__device__ __forceinline__ int sidx(int li, int lj) { return (lj + 1) * SX + li + 4; }  // li = i-i0, lj = j-j0
-}  // namespace fs
+namespace fs3 {
+constexpr int NC = 2;                  // cells per thread along x: lane and lane + 32
+constexpr int TX = 32 * NC, BY = 8;    // owned tile 64 x 8
+constexpr int NW = 10;                 // warps 0..7 own the tile rows, 8: +y halo row, 9: +x halo column
+constexpr int NT = 32 * NW;
+constexpr int BXW = TX + 8, BYH = BY + 2;  // TMA box 72 x 10: x in [i0-4, i0+68), y in [j0-1, j0+9)
+constexpr int BOX = BXW * BYH;
+constexpr int NARR = 7;                // ex ey ez bx by bz sigma
+// ring stride of one box: rounded up to 128 bytes so every TMA destination is 128-byte aligned
+template <typename T> __host__ __device__ constexpr int boxs() { return (int)(((BOX * sizeof(T) + 127) / 128) * 128 / sizeof(T)); }
+constexpr int RING = 4;                // planes in flight
+constexpr int XR = BY + 2, XC = TX + 2;  // exchange planes of the new fields
+enum { AEX = 0, AEY, AEZ, ABX, ABY, ABZ, ASG };
+template <typename T> __host__ __device__ constexpr size_t smem_bytes() {
+    return (size_t)RING * NARR * boxs<T>() * sizeof(T) + 3 * 2 * XR * XC * sizeof(T) + 2 * BOX * sizeof(T) + RING * 8 + 16;
+}
+template <typename T> size_t smem_bytes_n(int N) {  // plus the z tables
+    return ((smem_bytes<T>() + 3 * (size_t)(N + 3) * sizeof(T)) + 15) / 16 * 16;
+}
+}  // namespace fs3
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: gives up after ~1e6 polls (each poll may suspend for a while)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
+    for (int it = 0; it < (1 << 20); it++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// reciprocal used by the E update: one MUFU op in FP32 (about 1 ulp), exact division in FP64
+template <typename T> __device__ __forceinline__ T rcp_fast(T x);
+template <> __device__ __forceinline__ float rcp_fast<float>(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+template <> __device__ __forceinline__ double rcp_fast<double>(double x) { return 1.0 / x; }
+
+// per-thread state of the sweep (NC cells per thread); sweep_plane<PH>() advances
+// one z-plane with PH = (ktop - k) mod 4, so ring slots and exchange parities
+// are compile-time constants
+template <typename T> struct SweepThread {
+    T *ring, *x_ez, *x_bxn, *x_byn;
+    uint64_t *bars;
+    int *s_flag;
+    const CUtensorMap *maps;
+    unsigned plane_bytes;
+    int j, PS, N, k0, k1, klow, ktop, tid, i0, j0;
+    T rdy2, rdy, fy;  // per row: 1/(dy[j-1]+dy[j]), 1/dy[j], dtb/dy[j]
+    // per cell
+    int so[fs3::NC], xo[fs3::NC], i[fs3::NC], col[fs3::NC];
+    bool own[fs3::NC], vEx[fs3::NC], vEy[fs3::NC], vEz[fs3::NC];
+    T rdx2[fs3::NC], rdx[fs3::NC], fx[fs3::NC];
+    T oc0[fs3::NC], oci[fs3::NC], ocj[fs3::NC], od0[fs3::NC], odi[fs3::NC], odj[fs3::NC];  // Bz chunk offsets
+    T ex1[fs3::NC], ey1[fs3::NC], exn[fs3::NC], eyn[fs3::NC], ezn[fs3::NC];
+    T bxo1[fs3::NC], byo1[fs3::NC], bxn[fs3::NC], byn[fs3::NC], acc[fs3::NC];
+    T sxk[fs3::NC], syk[fs3::NC], szk[fs3::NC], bxk[fs3::NC], byk[fs3::NC];  // sigma sums and own B of plane k
+};
+
+template <typename T, int PH>
+__device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned rp, const StepScalars<T> &s,
+                                            const T *__restrict__ zt, const FieldSet<T> &out,
+                                            const SourceTable<T> &src, bool src_tile) {
+    using namespace fs3;
+    constexpr int BS = boxs<T>();
+    constexpr int S0 = PH, S1 = (PH + 1) & 3;
+    constexpr int QE = PH & 1, QB = (PH + 1) & 1;
+    constexpr int XP2 = XR * XC;
+    const int zi = k - t.klow;  // z tables: rdz, rdzs, dzk of plane klow + zi
+    // ---- B_new(k+1) from E_new(k+1) (own + neighbours) and E_new(k+2)
+    const bool doB = k + 1 < t.k1;
+    if (doB) {
+        const T fz = zt[3 * (zi + 1)] * s.dtb;  // dtb / dz(k+1)
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const T ezj = t.x_ez[QB * XP2 + t.xo[c] + XC], ezi = t.x_ez[QB * XP2 + t.xo[c] + 1];
+            const T bx = t.bxo1[c] + (t.ey1[c] - t.eyn[c]) * fz - (ezj - t.ezn[c]) * t.fy;
+            const T by = t.byo1[c] + (ezi - t.ezn[c]) * t.fx[c] - (t.ex1[c] - t.exn[c]) * fz;
+            t.bxn[c] = t.vEy[c] ? bx : t.bxo1[c];
+            t.byn[c] = t.vEx[c] ? by : t.byo1[c];
+            if (t.own[c]) {
+                const int o = t.col[c] + (k + 2) * t.PS;
+                out.bx[o] = t.bxn[c];
+                out.by[o] = t.byn[c];
+            }
+        }
+    }
+    // ---- E_new(k)
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        t.ex1[c] = t.exn[c];
+        t.ey1[c] = t.eyn[c];
+    }
+    if (k >= t.k0) {
+        const bool upd = k < t.N, lo = k < t.k1;
+        const T rzs = zt[3 * zi + 1];
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const T *p0 = t.ring + S0 * NARR * BS + t.so[c], *p1 = t.ring + S1 * NARR * BS + t.so[c];
+            const T a1 = p1[ASG * BS], b1 = p1[ASG * BS - 1], c1 = p1[ASG * BS - BXW], d1 = p1[ASG * BS - BXW - 1];
+            const T bym = p1[ABY * BS], bxm = p1[ABX * BS];
+            const T sx1 = a1 + c1, sy1 = a1 + b1, sz1 = sx1 + b1 + d1;
+            const T exo = p0[AEX * BS], eyo = p0[AEY * BS], ezo = p0[AEZ * BS];
+            if (upd) {
+                const T bz = p0[ABZ * BS] + (lo ? t.oc0[c] : t.od0[c]);
+                const T bzi = p0[ABZ * BS - 1] + (lo ? t.oci[c] : t.odi[c]);
+                const T bzj = p0[ABZ * BS - BXW] + (lo ? t.ocj[c] : t.odj[c]);
+                const T byi = p0[ABY * BS - 1], bxj = p0[ABX * BS - BXW];
+                // DuFort-Frankel update (ElectricalFiled.cu:89-345) of the three components, computed for
+                // every cell and kept where the component is updated; s.dt carries the 1/4 of the sigma sums
+                const T sdx = (t.sxk[c] + sx1) * s.dt, sdy = (t.syk[c] + sy1) * s.dt, sdz = t.szk[c] * s.dt;
+                const T rx = rcp_fast(s.lam2 + sdx), ry = rcp_fast(s.lam2 + sdy), rz = rcp_fast(s.lam2 + sdz);
+                const T cx = (bz - bzj) * t.rdy2 - (t.byk[c] - bym) * rzs;
+                const T cy = (t.bxk[c] - bxm) * rzs - (bz - bzi) * t.rdx2[c];
+                const T cz = (t.byk[c] - byi) * t.rdx2[c] - (t.bxk[c] - bxj) * t.rdy2;
+                const T ex = ((s.lam2 - sdx) * rx) * exo + (s.c4 * rx) * cx;
+                const T ey = ((s.lam2 - sdy) * ry) * eyo + (s.c4 * ry) * cy;
+                const T ez = ((s.lam2 - sdz) * rz) * ezo + (s.c4 * rz) * cz;
+                t.exn[c] = t.vEx[c] ? ex : exo;
+                t.eyn[c] = t.vEy[c] ? ey : eyo;
+                t.ezn[c] = t.vEz[c] ? ez : ezo;
+            } else {
+                t.exn[c] = exo;
+                t.eyn[c] = eyo;
+                t.ezn[c] = ezo;
+            }
+            t.bxo1[c] = t.bxk[c];  // B_old(k) for the next plane's B update
+            t.byo1[c] = t.byk[c];
+            t.bxk[c] = bxm;
+            t.byk[c] = bym;
+            t.sxk[c] = sx1;
+            t.syk[c] = sy1;
+            t.szk[c] = sz1;
+        }
+        if (upd && src_tile && s.wave != T(0)) {  // AddTx_*: subtracted after the update of the cell
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                if (!(t.vEx[c] || t.vEy[c])) continue;
+                for (int q = 0; q < src.nseg; q++) {
+                    const int cp = src.comp[q];
+                    int d;
+                    if (cp == 0) { if (t.j != src.j[q] || k != src.k[q]) continue; d = t.i[c] - src.i[q]; }
+                    else if (cp == 1) { if (t.i[c] != src.i[q] || k != src.k[q]) continue; d = t.j - src.j[q]; }
+                    else { if (t.i[c] != src.i[q] || t.j != src.j[q]) continue; d = k - src.k[q]; }
+                    if (d < 0 || d >= src.count[q]) continue;
+                    const T v = s.wave * src.coef[src.off[q] + d];
+                    if (cp == 0) t.exn[c] -= v; else if (cp == 1) t.eyn[c] -= v; else t.ezn[c] -= v;
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            if (upd && lo && t.own[c]) {
+                const int o = t.col[c] + (k + 1) * t.PS;
+                out.ex[o] = t.exn[c];
+                out.ey[o] = t.eyn[c];
+                out.ez[o] = t.ezn[c];
+            }
+            t.x_ez[QE * XP2 + t.xo[c]] = t.ezn[c];  // publish Ez_new(k)
+        }
+    }
+    if (doB) {  // publish B_new(k+1)
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            t.x_bxn[QB * XP2 + t.xo[c]] = t.bxn[c];
+            t.x_byn[QB * XP2 + t.xo[c]] = t.byn[c];
+        }
+    }
+    // plane k-2 is read by the next plane
+    if (k - 2 >= t.klow && !mbar_wait_bounded(t.bars + ((PH + 2) & 3), rp ^ (unsigned)((PH + 2) >> 2))) *t.s_flag = 1;
+    __syncthreads();
+    if (*t.s_flag) {  // a copy did not arrive: let the copies still in flight (planes k-2, k-3) land first
+        if (t.tid == 0) {
+            if (k - 2 >= t.klow) mbar_wait_bounded(t.bars + ((PH + 2) & 3), rp ^ (unsigned)((PH + 2) >> 2));
+            if (k - 3 >= t.klow) mbar_wait_bounded(t.bars + ((PH + 3) & 3), rp ^ (unsigned)((PH + 3) >> 2));
+        }
+        return false;
+    }
+    // plane k is no longer read: its ring slot takes plane k-4
+    if (t.tid == 0 && k - RING >= t.klow && k >= t.k0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        uint64_t *b = t.bars + S0;
+        mbar_expect_tx(b, t.plane_bytes);
+#pragma unroll
+        for (int a = 0; a < NARR; a++) tma_load_3d(t.ring + (S0 * NARR + a) * BS, t.maps + a, t.i0, t.j0, k - RING + 1, b);
+    }
+    // ---- Bz(k+1) = Bz(k+2) + dz (dBx/dx + dBy/dy)
+    if (doB) {
+        const T dz = zt[3 * (zi + 1) + 2];
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            t.acc[c] += dz * ((t.x_bxn[QB * XP2 + t.xo[c] + 1] - t.bxn[c]) * t.rdx[c] +
+                              (t.x_byn[QB * XP2 + t.xo[c] + XC] - t.byn[c]) * t.rdy);
+            if (t.own[c]) out.bz[t.col[c] + (k + 2) * t.PS] = t.acc[c];
+        }
+    }
+    return true;
+}
 
 template <typename T>
-__global__ void __launch_bounds__(fs::NT) k_fused_sweep(Geom g, FieldSet<T> in, FieldSet<T> out,
-                                                       const T *__restrict__ con, Axis<T> ax, StepScalars<T> sdir,
-                                                       const StepScalars<T> *__restrict__ table, StepGate gate,
-                                                       SourceTable<T> src) {
-    using namespace fs;
+__global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const __grid_constant__ SweepMaps maps, Geom g, FieldSet<T> out,
+                                                      const T *__restrict__ tin, T *__restrict__ tout, Axis<T> ax,
+                                                      StepScalars<T> sdir, const StepScalars<T> *__restrict__ table,
+                                                      StepGate gate, SourceTable<T> src, ZChunks zc, int *err) {
+    using namespace fs3;
     StepScalars<T> s = sdir;
     if (gate.base) {
         const long st = gate.step();
         if (st >= gate.nsteps) return;
         s = table[st];
     }
-    __shared__ T s_bx[2][SP], s_by[2][SP], s_sg[2][SP], s_bz[SP];
-    __shared__ T s_ex[2][SP], s_ey[2][SP], s_ez[SP], s_bxn[SP], s_byn[SP];
+    constexpr int BS = boxs<T>();
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SweepThread<T> t;
+    t.ring = reinterpret_cast<T *>(smem_raw);
+    t.x_ez = t.ring + RING * NARR * BS;  // [2][XR][XC]
+    t.x_bxn = t.x_ez + 2 * XR * XC;
+    t.x_byn = t.x_bxn + 2 * XR * XC;
+    T *s_oc = t.x_byn + 2 * XR * XC;  // [BYH][BXW] chunk offsets of Bz for planes < k1
+    T *s_oc1 = s_oc + BOX;            // ... for plane k1
+    t.bars = reinterpret_cast<uint64_t *>(s_oc1 + BOX);  // 8-byte aligned: every region above has an even size
+    t.s_flag = reinterpret_cast<int *>(t.bars + RING);
+    T *s_z = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(t.bars) + RING * 8 + 16);  // [N+3][3]
+    t.maps = maps.m;
 
-    const int tid = threadIdx.x;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-    const int L = g.L, M = g.M, N = g.N;
-    const long long PS = g.PS, XP = g.XP;
-
-    // region elements handled by this thread (load phase)
-    int rs[2];
-    long long rg[2];
-    bool rv[2];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    t.tid = tid;
+    t.i0 = blockIdx.x * TX;
+    t.j0 = blockIdx.y * BY;
+    const int L = g.L, M = g.M, N = g.N, XP = g.XP;
+    t.N = N;
+    t.PS = (int)g.PS;
+    const int c = blockIdx.z;
+    t.k0 = (c * N) / zc.n;  // = zc.kb[c]
+    t.k1 = ((c + 1) * N) / zc.n;
+    const int ty = w < 9 ? w : lane;
+    t.j = t.j0 + ty;
+    const bool rowok = w < 9 || lane <= BY;
+    t.rdy2 = (rowok && t.j >= 1 && t.j < M) ? ax.rdy2[t.j] : T(0);
+    t.rdy = (rowok && t.j < M) ? ax.rdy[t.j] : T(0);
+    t.fy = t.rdy * s.dtb;
 #pragma unroll
-    for (int q = 0; q < 2; q++) {
-        int e = tid + q * NT;
-        int li = e % RW - 1, lj = e / RW - 1;
-        int i = i0 + li, j = j0 + lj;
-        rv[q] = e < RN && i <= L && j <= M;
-        rs[q] = e < RN ? sidx(li, lj) : 0;
-        rg[q] = g.at(i, j, 0);
+    for (int q = 0; q < NC; q++) {
+        const int tx = w < 9 ? lane + 32 * q : TX;
+        const bool act = w < 9 || (q == 0 && lane <= BY);
+        const int i = t.i0 + tx;
+        t.i[q] = i;
+        t.own[q] = act && ty < BY && tx < TX && i < L && t.j < M;
+        t.col[q] = (t.j + 1) * XP + (i + 4);
+        t.so[q] = act ? (ty + 1) * BXW + (tx + 4) : BXW + 4;
+        t.xo[q] = act ? ty * XC + tx : XR * XC - 1;  // inactive slots publish into a cell nobody reads
+        t.vEx[q] = act && t.j >= 1 && t.j < M && i < L;
+        t.vEy[q] = act && i >= 1 && i < L && t.j < M;
+        t.vEz[q] = t.vEx[q] && i >= 1;
+        t.rdx2[q] = t.vEy[q] ? ax.rdx2[i] : T(0);
+        t.rdx[q] = (act && i < L) ? ax.rdx[i] : T(0);
+        t.fx[q] = t.rdx[q] * s.dtb;
     }
-    // E work items handled by this thread
-    int es[2], ei[2], ej[2];
-    long long eg[2];
-    bool ev[2];
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-        int e = tid + q * NT;
-        int li = e % EW, lj = e / EW;
-        ei[q] = i0 + li; ej[q] = j0 + lj;
-        ev[q] = e < EN;
-        es[q] = ev[q] ? sidx(li, lj) : 0;
-        eg[q] = g.at(ei[q], ej[q], 0);
+    t.ktop = t.k1 < N ? t.k1 : N;  // first plane: the chunk's halo plane below, or the zero bottom
+    t.klow = t.k0 - 1 >= -1 ? t.k0 - 1 : -1;
+    t.plane_bytes = (unsigned)(NARR * BOX * sizeof(T));
+    const int ktop = t.ktop, klow = t.klow;
+    s.dt *= T(0.25);  // the sweep forms sigma sums of four cells: 0.25 * sum * dt
+    for (int e = tid; e <= ktop + 1 - klow; e += NT) {
+        const int k = klow + e;
+        const bool in = k >= 0 && k < N;
+        s_z[3 * e] = in ? ax.rdz[k] : T(0);
+        s_z[3 * e + 1] = in ? ax.rdzs[k] : T(0);
+        s_z[3 * e + 2] = in ? ax.dzk[k] : T(0);
     }
-    const bool own = true;  // every thread owns exactly one cell of the TX x TY tile
-    const int oi = i0 + (tid % TX), oj = j0 + (tid / TX);
-    const int os = sidx(tid % TX, tid / TX);
-    const bool oin = oi < L && oj < M;
-    const long long og = g.at(oi, oj, 0);
-    const T o_rdx = oin ? ax.rdx[oi] : T(0), o_rdy = oin ? ax.rdy[oj] : T(0);
 
-    // zero the E(k+1) slot (plane N of Ex/Ey is the zero bottom)
-    for (int e = tid; e < SP; e += NT) { s_ex[1][e] = T(0); s_ey[1][e] = T(0); }
-    // prologue: B_old and sigma of the bottom plane straight into the "cur" slot
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-        if (tid + q * NT < RN) {
-            long long p = rg[q] + (long long)(N - 1) * PS;
-            s_bx[0][rs[q]] = rv[q] ? ldg(in.bx + p) : T(0);
-            s_by[0][rs[q]] = rv[q] ? ldg(in.by + p) : T(0);
-            s_sg[0][rs[q]] = rv[q] ? ldg(con + p) : T(0);
-        }
+    if (tid == 0) {
+        for (int r = 0; r < RING; r++) mbar_init(t.bars + r, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *t.s_flag = 0;
     }
-    // registers: region prefetch (Bx/By/sigma of plane k-1, Bz of plane k), E_old of plane k
-    T pbx[2], pby[2], psg[2], pbz[2], pex[2], pey[2], pez[2];
-    auto prefetch = [&](int k) {  // data for iteration k
+    __syncthreads();
+    if (tid == 0)  // planes ktop .. ktop-3 into slots 0..3
+        for (int p = ktop, q = 0; q < RING && p >= klow; p--, q++) {
+            uint64_t *b = t.bars + q;
+            mbar_expect_tx(b, t.plane_bytes);
+            for (int a = 0; a < NARR; a++) tma_load_3d(t.ring + (q * NARR + a) * BS, t.maps + a, t.i0, t.j0, p + 1, b);
+        }
+    // chunk offsets of Bz over the box (zero without chunking)
+    for (int e = tid; e < BOX; e += NT) {
+        T o = T(0), o1 = T(0);
+        if (zc.n > 1) {
+            const int gy = t.j0 + e / BXW, gx = t.i0 + e % BXW;  // padded coordinates
+            if (gy < g.YP && gx < XP) {
+                const int pc = gy * XP + gx;
+                for (int q = c + 1; q < zc.n; q++) o += ldg(tin + q * t.PS + pc);
+                o1 = c + 1 < zc.n ? o - ldg(tin + (c + 1) * t.PS + pc) : T(0);
+            }
+        }
+        s_oc[e] = o;
+        s_oc1[e] = o1;
+    }
+    {  // every thread observes the completion of the first two planes
+        bool ok = mbar_wait_bounded(t.bars + 0, 0u);
+        ok = ok && mbar_wait_bounded(t.bars + 1, 0u);
+        if (!ok) *t.s_flag = 1;
+    }
+    __syncthreads();
+    if (*t.s_flag) {  // record it, let the first planes land, leave together
+        if (tid == 0) {
+            atomicExch(err, 1);
+            for (int q = 0; q < RING && ktop - q >= klow; q++) mbar_wait_bounded(t.bars + q, 0u);
+        }
+        return;
+    }
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
-            long long pm = rg[q] + (long long)(k - 1) * PS, pk = rg[q] + (long long)k * PS;
-            pbx[q] = rv[q] ? ldg(in.bx + pm) : T(0);
-            pby[q] = rv[q] ? ldg(in.by + pm) : T(0);
-            psg[q] = rv[q] ? ldg(con + pm) : T(0);
-            pbz[q] = rv[q] ? ldg(in.bz + pk) : T(0);
-            bool ok = ev[q] && ei[q] <= L && ej[q] <= M;
-            long long pe = eg[q] + (long long)k * PS;
-            pex[q] = ok ? ldg(in.ex + pe) : T(0);
-            pey[q] = ok ? ldg(in.ey + pe) : T(0);
-            pez[q] = ok ? ldg(in.ez + pe) : T(0);
-        }
-    };
-    prefetch(N - 1);
+    for (int q = 0; q < NC; q++) {
+        const int so = t.so[q];
+        t.oc0[q] = s_oc[so]; t.oci[q] = s_oc[so - 1]; t.ocj[q] = s_oc[so - BXW];
+        t.od0[q] = s_oc1[so]; t.odi[q] = s_oc1[so - 1]; t.odj[q] = s_oc1[so - BXW];
+        const T *p0 = t.ring + so;  // carried values of plane ktop (slot 0)
+        const T a = p0[ASG * BS], b = p0[ASG * BS - 1], cc = p0[ASG * BS - BXW], d = p0[ASG * BS - BXW - 1];
+        t.sxk[q] = a + cc;
+        t.syk[q] = a + b;
+        t.szk[q] = a + cc + b + d;
+        t.bxk[q] = p0[ABX * BS];
+        t.byk[q] = p0[ABY * BS];
+        t.ex1[q] = t.ey1[q] = t.exn[q] = t.eyn[q] = t.ezn[q] = T(0);
+        t.bxo1[q] = t.byo1[q] = t.bxn[q] = t.byn[q] = t.acc[q] = T(0);
+    }
+    bool src_tile = false;  // tile-uniform: does any source segment touch this tile?
+    for (int q = 0; q < src.nseg; q++) {
+        int a0 = src.i[q], a1 = src.i[q], b0 = src.j[q], b1 = src.j[q];
+        if (src.comp[q] == 0) a1 += src.count[q] - 1;
+        if (src.comp[q] == 1) b1 += src.count[q] - 1;
+        if (a1 >= t.i0 && a0 <= t.i0 + TX && b1 >= t.j0 && b0 <= t.j0 + BY) src_tile = true;
+    }
 
-    T acc = T(0);
-    int cur = 0, ecur = 0;
-    for (int k = N - 1; k >= 0; k--) {
-        const int nxt = cur ^ 1, eprev = ecur ^ 1;
-        // phase 1: publish the prefetched planes, keep E_old(k), prefetch k-1
-        T cex[2], cey[2], cez[2];
+    bool ok = true;
+    unsigned rp = 0;  // parity of the ring round
+    for (int k = ktop; ok && k >= t.k0 - 1; k -= RING, rp ^= 1u) {
+        ok = sweep_plane<T, 0>(t, k, rp, s, s_z, out, src, src_tile);
+        if (!ok || k - 1 < t.k0 - 1) break;
+        ok = sweep_plane<T, 1>(t, k - 1, rp, s, s_z, out, src, src_tile);
+        if (!ok || k - 2 < t.k0 - 1) break;
+        ok = sweep_plane<T, 2>(t, k - 2, rp, s, s_z, out, src, src_tile);
+        if (!ok || k - 3 < t.k0 - 1) break;
+        ok = sweep_plane<T, 3>(t, k - 3, rp, s, s_z, out, src, src_tile);
+    }
+    if (!ok) {  // a copy did not arrive (the copies in flight were drained in sweep_plane)
+        if (tid == 0) atomicExch(err, 1);
+        return;
+    }
+    if (zc.n > 1) {
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
-            if (tid + q * NT < RN) {
-                s_bx[nxt][rs[q]] = pbx[q];
-                s_by[nxt][rs[q]] = pby[q];
-                s_sg[nxt][rs[q]] = psg[q];
-                s_bz[rs[q]] = pbz[q];
-            }
-            cex[q] = pex[q]; cey[q] = pey[q]; cez[q] = pez[q];
-        }
-        if (k > 0) prefetch(k - 1);
-        __syncthreads();
-
-        // phase 2: E(k) on the (TX+1) x (TY+1) work region
-        const T rzs = ax.rdzs[k];
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            if (!ev[q]) continue;
-            const int i = ei[q], j = ej[q], c = es[q];
-            T ex = cex[q], ey = cey[q], ez = cez[q];
-            const bool inx = i < L, iny = j < M;
-            if (inx && iny && j >= 1) {
-                T sg = T(0.5) * (T(0.5) * (s_sg[cur][c - SX] + s_sg[cur][c]) + T(0.5) * (s_sg[nxt][c - SX] + s_sg[nxt][c]));
-                T curl = (s_bz[c] - s_bz[c - SX]) * ax.rdy2[j] - (s_by[cur][c] - s_by[nxt][c]) * rzs;
-                ex = df_update(s, sg, ex, curl);
-            }
-            if (inx && iny && i >= 1) {
-                T sg = T(0.25) * (s_sg[cur][c - 1] + s_sg[cur][c] + s_sg[nxt][c - 1] + s_sg[nxt][c]);
-                T curl = (s_bx[cur][c] - s_bx[nxt][c]) * rzs - (s_bz[c] - s_bz[c - 1]) * ax.rdx2[i];
-                ey = df_update(s, sg, ey, curl);
-            }
-            if (inx && iny && i >= 1 && j >= 1) {
-                T sg = T(0.25) * (s_sg[cur][c - SX - 1] + s_sg[cur][c - SX] + s_sg[cur][c - 1] + s_sg[cur][c]);
-                T curl = (s_by[cur][c] - s_by[cur][c - 1]) * ax.rdx2[i] - (s_bx[cur][c] - s_bx[cur][c - SX]) * ax.rdy2[j];
-                ez = df_update(s, sg, ez, curl);
-            }
-            if (s.wave != T(0)) {  // AddTx_*: subtract after the update of the cell
-                for (int sgi = 0; sgi < src.nseg; sgi++) {
-                    const int cp = src.comp[sgi];
-                    int q0;
-                    if (cp == 0) { if (j != src.j[sgi] || k != src.k[sgi]) continue; q0 = i - src.i[sgi]; }
-                    else if (cp == 1) { if (i != src.i[sgi] || k != src.k[sgi]) continue; q0 = j - src.j[sgi]; }
-                    else { if (i != src.i[sgi] || j != src.j[sgi]) continue; q0 = k - src.k[sgi]; }
-                    if (q0 < 0 || q0 >= src.count[sgi]) continue;
-                    T v = s.wave * src.coef[src.off[sgi] + q0];
-                    if (cp == 0) ex -= v; else if (cp == 1) ey -= v; else ez -= v;
-                }
-            }
-            s_ex[ecur][c] = ex; s_ey[ecur][c] = ey; s_ez[c] = ez;
-            if (i - i0 < TX && j - j0 < TY && inx && iny) {
-                long long p = eg[q] + (long long)k * PS;
-                out.ex[p] = ex; out.ey[p] = ey; out.ez[p] = ez;
-            }
-        }
-        __syncthreads();
-
-        // phase 3: Bx on [i0, i0+TX] x [j0, j0+TY), By on [i0, i0+TX) x [j0, j0+TY]
-        const T rdz = ax.rdz[k], dtb = s.dtb;
-        for (int e = tid; e < (TX + 1) * TY + TX * (TY + 1); e += NT) {
-            if (e < (TX + 1) * TY) {
-                int li = e % (TX + 1), lj = e / (TX + 1), i = i0 + li, j = j0 + lj, c = sidx(li, lj);
-                T b = s_bx[cur][c];
-                if (i >= 1 && i < L && j < M)
-                    b += ((s_ey[eprev][c] - s_ey[ecur][c]) * rdz - (s_ez[c + SX] - s_ez[c]) * ax.rdy[j]) * dtb;
-                s_bxn[c] = b;
-                if (li < TX && i < L && j < M) out.bx[g.at(i, j, k)] = b;
-            } else {
-                int e2 = e - (TX + 1) * TY;
-                int li = e2 % TX, lj = e2 / TX, i = i0 + li, j = j0 + lj, c = sidx(li, lj);
-                T b = s_by[cur][c];
-                if (j >= 1 && j < M && i < L)
-                    b += ((s_ez[c + 1] - s_ez[c]) * ax.rdx[i] - (s_ex[eprev][c] - s_ex[ecur][c]) * rdz) * dtb;
-                s_byn[c] = b;
-                if (lj < TY && i < L && j < M) out.by[g.at(i, j, k)] = b;
-            }
-        }
-        __syncthreads();
-
-        // phase 4: Bz(k) = Bz(k+1) + dz (dBx/dx + dBy/dy), owned cells
-        if (own) {
-            acc += ax.dzk[k] * ((s_bxn[os + 1] - s_bxn[os]) * o_rdx + (s_byn[os + SX] - s_byn[os]) * o_rdy);
-            if (oin) out.bz[og + (long long)k * PS] = acc;
-        }
-        cur = nxt;
-        ecur = eprev;
+        for (int q = 0; q < NC; q++)
+            if (t.own[q]) tout[c * t.PS + t.col[q]] = t.acc[q];
     }
 }
 
 template <typename T>
-void launch_fused_sweep(const Geom &g, FieldSet<T> in, FieldSet<T> out, const T *con, const Axis<T> &ax,
-                        StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
-                        const SourceTable<T> &src, cudaStream_t st) {
-    dim3 grd((g.L + fs::TX - 1) / fs::TX, (g.M + fs::TY - 1) / fs::TY);
-    k_fused_sweep<T><<<grd, fs::NT, 0, st>>>(g, in, out, con, ax, s, table, gate, src);
+void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
+                        const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
+                        const SourceTable<T> &src, const ZChunks &zc, int *err, cudaStream_t st) {
+    dim3 grd((g.L + fs3::TX - 1) / fs3::TX, (g.M + fs3::BY - 1) / fs3::BY, zc.n);
+    k_sweep<T><<<grd, fs3::NT, fs3::smem_bytes_n<T>(g.N), st>>>(maps, g, out, tin, tout, ax, s, table, gate, src, zc, err);
+}
+
+template <typename T> cudaError_t sweep_configure(int N) {
+    return cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs3::smem_bytes_n<T>(N));
+}
+template <typename T> size_t sweep_smem_bytes(int N) { return fs3::smem_bytes_n<T>(N); }
+int sweep_box_x() { return fs3::BXW; }
+int sweep_box_y() { return fs3::BYH; }
+
+// materialise Bz = P + O_c in place and clear the chunk totals
+template <typename T>
+__global__ void k_bz_consolidate(Geom g, T *bz, T *tot, ZChunks zc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > g.L || j > g.M || zc.n <= 1) return;
+    const int XP = g.XP, PS = (int)g.PS, plane = (g.M + 2) * XP;
+    const int col = (j + 1) * XP + (i + 4);
+    T o = T(0);
+    for (int c = zc.n - 1; c >= 0; c--) {
+        for (int k = zc.kb[c]; k < zc.kb[c + 1]; k++) bz[col + (k + 1) * PS] += o;
+        o += tot[c * plane + col];
+        tot[c * plane + col] = T(0);
+    }
+}
+
+template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, const ZChunks &zc, cudaStream_t st) {
+    if (zc.n <= 1) return;
+    dim3 blk(32, 8), grd((g.L + 1 + 31) / 32, (g.M + 1 + 7) / 8);
+    k_bz_consolidate<T><<<grd, blk, 0, st>>>(g, bz, tot, zc);
 }
 
 #define INST(T)                                                                                                    \
     template void launch_update_e<T>(const Geom &, FieldSet<T>, const T *, const Axis<T> &, StepScalars<T>,        \
                                      const SourceTable<T> &, cudaStream_t);                                        \
     template void launch_bderivate<T>(const Geom &, FieldSet<T>, const Axis<T> &, T, cudaStream_t);                \
-    template void launch_fused_sweep<T>(const Geom &, FieldSet<T>, FieldSet<T>, const T *, const Axis<T> &,        \
-                                        StepScalars<T>, const StepScalars<T> *, StepGate,                          \
-                                        const SourceTable<T> &, cudaStream_t);
+    template void launch_fused_sweep<T>(const SweepMaps &, const Geom &, FieldSet<T>, const T *, T *,             \
+                                        const Axis<T> &, StepScalars<T>, const StepScalars<T> *, StepGate,         \
+                                        const SourceTable<T> &, const ZChunks &, int *, cudaStream_t);             \
+    template cudaError_t sweep_configure<T>(int);                                                                  \
+    template size_t sweep_smem_bytes<T>(int);                                                                      \
+    template void launch_bz_consolidate<T>(const Geom &, T *, T *, const ZChunks &, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

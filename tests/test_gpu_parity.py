@@ -102,10 +102,11 @@ def test_upcontinuation_stage(built, case_dir, name, precision):
         assert rel(sim.get(n), orc.get(n)) < BOUNDARY_TOL[precision], n
 
 
+@pytest.mark.parametrize("zchunks", [1, 3])
 @pytest.mark.parametrize("precision", [64, 32])
 @pytest.mark.parametrize("name", ["tiny", "small", "txvar"])
-def test_fused_sweep_equals_e_then_b(built, case_dir, name, precision):
-    sim, orc = pair(case_dir, name, precision)
+def test_fused_sweep_equals_e_then_b(built, case_dir, name, precision, zchunks):
+    sim, orc = pair(case_dir, name, precision, zchunks=zchunks)
     sched = orc.schedule()
     for step in (5, 260):
         randomize(sim, orc, 31 + step)
@@ -147,9 +148,10 @@ def trace_error(got, exp):
     return worst
 
 
+@pytest.mark.parametrize("zchunks", [0, 1, 4])
 @pytest.mark.parametrize("name", ["tiny", "small"])
-def test_full_run_fp64_matches_oracle(built, case_dir, name):
-    sim, orc = pair(case_dir, name, 64)
+def test_full_run_fp64_matches_oracle(built, case_dir, name, zchunks):
+    sim, orc = pair(case_dir, name, 64, zchunks=zchunks)
     exp, n = orc.run(0)
     got = sim.run(0, nr=exp.shape[0])
     assert n == sim.info["nsteps"]
@@ -193,6 +195,30 @@ def test_stepwise_advance_equals_run(built, case_dir):
     while not done:
         done = sim.advance(16)
     np.testing.assert_array_equal(sim.traces(nr), ref)
+
+
+def test_two_fused_steps_with_chunks_then_stage_api(built, case_dir):
+    """Chunk-partial Bz must be consistent for every consumer: boundary, E stage, receivers."""
+    sim, orc = pair(case_dir, "small", 64, zchunks=3)
+    sched = orc.schedule()
+    randomize(sim, orc, 77)
+    for step in (40, 41):
+        lam, dt, dtb, wave = sched["lam"][step], sched["dt1"][step], 0.5 * (sched["dt1"][step] + sched["dt2"][step]), sched["wave"][step]
+        sim.select_tx(0)
+        sim.upcontinuation()
+        orc.upcontinuation()
+        sim.fused_step(lam, dt, dtb, wave)
+        orc.electric_field(0, lam, dt, wave)
+        orc.bderivate(dtb)
+    iv, _, rxn = orc.tx(0)
+    nr = int(iv[1])
+    got = sim.rx_sample(0, 1, nr)
+    exp = [[orc.rx_interp(c, int(r) - 1) for r in rxn] for c in (3, 4, 5)]
+    assert rel(got[orc.nefcmp:], np.array(exp)) < 1e-9
+    sim.electric_field(sched["lam"][42], sched["dt1"][42], 0.0)
+    orc.electric_field(0, sched["lam"][42], sched["dt1"][42], 0.0)
+    for n in ("Ex", "Ey", "Ez", "Bz", "BxAir", "ByAir"):
+        assert rel(sim.get(n), orc.get(n)) < 1e-9, n
 
 
 def test_repeat_runs_are_bitwise_identical(built, case_dir):
