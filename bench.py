@@ -260,7 +260,7 @@ def run_gb300(args, dist):
                    "steps_per_run": nsteps_total, "parallelism": f"replicas{dist.world}",
                    "l2": "working set 13 x %.0f MB volume arrays > 129 MB L2, no flush needed"
                          % (cells * 4 * 1.13 / 1e6)},
-        "gpu_launches": K * 6 + math.ceil(K / 64),
+        "gpu_launches": K * info2["launches_per_step"] + math.ceil(K / 64),
         "roofline": {"bound": "hbm", "kernel": "k_fused_sweep", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(args.workload), "ms_per_launch": ms_sweep,

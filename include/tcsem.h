@@ -49,7 +49,9 @@ typedef struct {
     int fix_dual_bipole;  /* 1: inject the second bipole of ort=5 at its own cells (default 0 = as the reference) */
     int graph_steps;      /* steps per captured CUDA graph, 0 = default (even numbers only) */
     int zchunks;          /* z-chunks of the fused sweep, 0 = chosen from the grid and the GPU */
-    int reserved[3];
+    int serial_boundary;  /* 1: boundary pipeline strictly before the whole sweep; default 0 = the
+                             boundary and the top z-chunk run beside the lower chunks */
+    int reserved[2];
 } tcsem_opts;
 
 typedef struct {
@@ -59,6 +61,7 @@ typedef struct {
     long nsteps;          /* time steps of one transmitter run */
     int precision;
     size_t device_bytes;  /* device memory held by the handle */
+    int launches_per_step; /* kernels launched per time step by tcsem_advance */
 } tcsem_info;
 
 /* Opening a survey.  tcsem_open_dir reads FDTD_setup.in, Cond.bin, Receiver.in

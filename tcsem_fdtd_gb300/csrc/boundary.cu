@@ -9,7 +9,8 @@
 // pipeline instead
 //   1. remaps each of the M old rows to L1 uniform points with dense spline
 //      weights (precomputed from the same natural-spline rule) and FFTs it
-//      along x -- M rows, not M1;
+//      along x -- M rows, not M1, two real rows packed in one complex
+//      transform;
 //   2. per x-frequency column: applies Py in the x-frequency domain, FFTs
 //      along y, multiplies by the two continuation filters, inverse-FFTs
 //      along y and keeps only the rows the final bilinear remap samples;
@@ -20,179 +21,294 @@
 // length written here (no cuFFT).
 #include "kernels.cuh"
 #include "boundary.cuh"
+#include "fft.cuh"
 
 namespace tcsem {
 
-template <typename T> __device__ __forceinline__ C2<T> cmul(C2<T> a, C2<T> b) {
-    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
-}
-template <typename T> __device__ __forceinline__ C2<T> cadd(C2<T> a, C2<T> b) { return {a.x + b.x, a.y + b.y}; }
+constexpr int kBndThreads = 256;
 
-// twiddle W_n^e = exp(-+2 pi i e / n) from the forward table
-template <typename T> __device__ __forceinline__ C2<T> twid(const C2<T> *tw, int e, bool inv) {
-    C2<T> w = tw[e];
-    if (inv) w.y = -w.y;
-    return w;
-}
-
-// Stockham autosort FFT of length P.n held in shared memory.  Radices up to 8
-// run one butterfly per thread; larger prime radices compute each output
-// directly.  Returns the buffer that holds the result.
+// Natural-spline second derivatives mb[0..n) of the line y[0..n) (stride ys)
+// from the precomputed elimination factors tab = g | w | inv | du; one thread
+// per line (n is at most 128).
 template <typename T>
-__device__ C2<T> *fft_smem(C2<T> *a, C2<T> *b, const FFTPlan &P, const C2<T> *__restrict__ tw, bool inv) {
-    const int n = P.n, tid = threadIdx.x, nth = blockDim.x;
-    int Ns = 1;
-    for (int s = 0; s < P.nst; s++) {
-        const int p = P.radix[s], m = n / p, step = n / (Ns * p);
-        if (p <= 8) {
-            for (int r = tid; r < m; r += nth) {
-                const int lo = r % Ns, base = (r / Ns) * Ns * p + lo, st = step * lo;
-                C2<T> v[8];
-#pragma unroll
-                for (int q = 0; q < 8; q++)
-                    if (q < p) v[q] = a[r + q * m];
-#pragma unroll
-                for (int q = 1; q < 8; q++)
-                    if (q < p) v[q] = cmul(v[q], twid(tw, (q * st) % n, inv));
-#pragma unroll
-                for (int u = 0; u < 8; u++) {
-                    if (u >= p) break;
-                    C2<T> acc = v[0];
-#pragma unroll
-                    for (int q = 1; q < 8; q++)
-                        if (q < p) acc = cadd(acc, cmul(v[q], twid(tw, ((q * u) % p) * m, inv)));
-                    b[base + u * Ns] = acc;
-                }
-            }
-        } else {
-            for (int o = tid; o < n; o += nth) {
-                const int hi = o / (Ns * p), rem = o % (Ns * p), u = rem / Ns, lo = rem % Ns, r = hi * Ns + lo;
-                const int st = ((lo + u * Ns) * step) % n;
-                C2<T> acc = {T(0), T(0)};
-                int e = 0;
-                for (int q = 0; q < p; q++) {
-                    acc = cadd(acc, cmul(a[r + q * m], twid(tw, e, inv)));
-                    e += st;
-                    if (e >= n) e -= n;
-                }
-                b[o] = acc;
-            }
+__device__ void spline_solve(const T *__restrict__ tab, int n, const T *y, int ys, T *mb) {
+    const T *g = tab, *w = tab + n, *inv = tab + 2 * n, *du = tab + 3 * n;
+    T yc = y[ys], dprev = (yc - y[0]) * g[0], rp = T(0);
+    mb[0] = T(0);
+#pragma unroll 4
+    for (int i = 1; i < n - 1; i++) {
+        const T yn = y[(i + 1) * ys], dc = (yn - yc) * g[i];
+        rp = (dc - dprev) - w[i] * rp;
+        mb[i] = rp;
+        dprev = dc;
+        yc = yn;
+    }
+    T m = T(0);
+    mb[n - 1] = m;
+#pragma unroll 4
+    for (int i = n - 2; i >= 1; i--) {
+        m = (mb[i] - du[i] * m) * inv[i];
+        mb[i] = m;
+    }
+}
+
+// one remapped point from its three-node window (y and mb start at the window)
+template <typename T>
+__device__ __forceinline__ T spline_out(const T *c, int npts, const T *y, int ys, const T *mb) {
+    return c[0] * y[0] + c[npts] * y[ys] + c[2 * npts] * y[2 * ys] + c[3 * npts] * mb[0] + c[4 * npts] * mb[1] +
+           c[5 * npts] * mb[2];
+}
+
+// Shared-memory layouts (byte offsets from a 128-byte aligned base), used by
+// the kernels and by the host for the launch size.  Every region starts on a
+// 16-byte boundary so the bulk copies can land in it.
+struct RowsFwdLayout { size_t bar, tw, tab, tabi, row, a, b, mb, total; };
+struct ColsLayout { size_t bar, tw, tab, tabi, col, gx, gy, a, b, mb, total; };
+struct RowsInvLayout { size_t bar, tw, vx, vy, a, b, total; };
+
+template <typename T> __host__ __device__ inline RowsFwdLayout rows_fwd_layout(const BoundaryDev<T> &bd, int L) {
+    RowsFwdLayout l{};
+    size_t o = 0;
+    l.bar = o; o += 16;
+    l.tw = o; o += rnd16(bd.L1 * sizeof(C2<T>));
+    l.tab = o; o += rnd16(bd.rx.nT * sizeof(T));
+    l.tabi = o; o += rnd16(bd.rx.nI * sizeof(int));
+    l.row = o; o += rnd16(2 * (size_t)L * sizeof(T));
+    l.a = o; o += rnd16(bd.L1 * sizeof(C2<T>));
+    l.b = o; o += rnd16(bd.L1 * sizeof(C2<T>));
+    l.mb = o; o += rnd16(4 * (size_t)bd.rx.nmax * sizeof(T));
+    l.total = o;
+    return l;
+}
+template <typename T> __host__ __device__ inline ColsLayout cols_layout(const BoundaryDev<T> &bd) {
+    ColsLayout l{};
+    size_t o = 0;
+    l.bar = o; o += 16;
+    l.tw = o; o += rnd16(bd.M1 * sizeof(C2<T>));
+    l.tab = o; o += rnd16(bd.ry.nT * sizeof(T));
+    l.tabi = o; o += rnd16(bd.ry.nI * sizeof(int));
+    l.col = o; o += rnd16(bd.M * sizeof(C2<T>));
+    l.gx = o; o += rnd16(bd.M1 * sizeof(T));
+    l.gy = o; o += rnd16(bd.M1 * sizeof(T));
+    l.a = o; o += rnd16(2 * (size_t)bd.M1 * sizeof(C2<T>));
+    l.b = o; o += rnd16(2 * (size_t)bd.M1 * sizeof(C2<T>));
+    l.mb = o; o += rnd16(4 * (size_t)bd.ry.nmax * sizeof(T));
+    l.total = o;
+    return l;
+}
+template <typename T> __host__ __device__ inline RowsInvLayout rows_inv_layout(const BoundaryDev<T> &bd) {
+    RowsInvLayout l{};
+    size_t o = 0;
+    l.bar = o; o += 16;
+    l.tw = o; o += rnd16(bd.L1 * sizeof(C2<T>));
+    l.vx = o; o += rnd16(bd.H * sizeof(C2<T>));
+    l.vy = o; o += rnd16(bd.H * sizeof(C2<T>));
+    l.a = o; o += rnd16(bd.L1 * sizeof(C2<T>));
+    l.b = o; o += rnd16(bd.L1 * sizeof(C2<T>));
+    l.total = o;
+    return l;
+}
+
+// every thread observes the bulk copies of phase 0 on bar; false (after
+// recording the error and letting the copies land) if any thread gave up
+__device__ __forceinline__ bool staged(uint64_t *bar, int *err) {
+    const bool ok = mbar_wait_bounded(bar, 0u);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            mbar_wait_bounded(bar, 0u);
         }
-        __syncthreads();
-        C2<T> *t = a; a = b; b = t;
-        Ns *= p;
+        return false;
     }
-    return a;
+    return true;
 }
 
-// ---- stage 1: x-remap of the M old rows + forward FFT along x
+// ---- stage 1: x-remap of the M old rows + forward FFT along x.  Rows j0 and
+// j0+1 travel as the real and imaginary parts of one complex transform and are
+// separated in the spectrum: X1 = (Z[k] + conj Z[-k]) / 2, X2 = (Z[k] - conj Z[-k]) / 2i.
+// Output FT is stored x-frequency major, FT[kx][j].
 template <typename T>
-__global__ void k_rows_fwd(BoundaryDev<T> bd, const T *__restrict__ bz, const T *__restrict__ tot, int nch, Geom g,
-                           StepGate gate) {
+__global__ void __launch_bounds__(kBndThreads) k_rows_fwd(BoundaryDev<T> bd, const T *__restrict__ bz,
+                                                          const T *__restrict__ tot, int nch, Geom g,
+                                                          StepGate gate) {
     if (gate.base && gate.step() >= gate.nsteps) return;
-    extern __shared__ unsigned char smem_raw[];
-    C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw);
-    C2<T> *b = a + bd.L1;
-    T *row = reinterpret_cast<T *>(b + bd.L1);
-    const int j = blockIdx.x, L = g.L;
-    const T *src = bz + g.at(0, j, 0);  // plane 0 of Bz (chunk-partial: add the totals of the chunks below)
-    const long long plane = (long long)(g.M + 2) * g.XP, col0 = (long long)(j + 1) * g.XP + 4;
-    for (int i = threadIdx.x; i < L; i += blockDim.x) {
-        T v = src[i];
-        for (int c = 1; c < nch; c++) v += tot[c * plane + col0 + i];
-        row[i] = v;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int L1 = bd.L1, L = g.L;
+    const AxisRemap<T> &R = bd.rx;
+    const RowsFwdLayout ly = rows_fwd_layout(bd, L);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + ly.bar);
+    C2<T> *tw = reinterpret_cast<C2<T> *>(smem_raw + ly.tw);
+    T *tab = reinterpret_cast<T *>(smem_raw + ly.tab);
+    int *tabi = reinterpret_cast<int *>(smem_raw + ly.tabi);
+    T *row = reinterpret_cast<T *>(smem_raw + ly.row);  // [2][L]
+    C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw + ly.a);
+    C2<T> *b = reinterpret_cast<C2<T> *>(smem_raw + ly.b);
+    T *mbuf = reinterpret_cast<T *>(smem_raw + ly.mb);  // [strip][row][nmax]
+    if (threadIdx.x == 0) {  // twiddles and remap tables in one bulk phase
+        const unsigned btw = (unsigned)rnd16(L1 * sizeof(C2<T>)), bt = (unsigned)rnd16(R.nT * sizeof(T)),
+                       bi = (unsigned)rnd16(R.nI * sizeof(int));
+        mbar_init(bar, 1);
+        mbar_init_fence();
+        mbar_expect_tx(bar, btw + bt + bi);
+        bulk_load(tw, bd.twx, btw, bar);
+        bulk_load(tab, R.tabT, bt, bar);
+        bulk_load(tabi, R.tabI, bi, bar);
     }
-    __syncthreads();
-    const int anl = bd.AnLx, nx = bd.Nx, AL = bd.AL;
-    for (int c = threadIdx.x; c < bd.L1; c += blockDim.x) {
-        T v;
-        if (c < anl) {  // left strip (Intep_BzIR2R_0x)
-            const T *w = bd.Wl + (size_t)c * bd.n1;
-            v = T(0);
-            for (int m = 0; m < bd.n1; m++) v += w[m] * row[m];
-        } else if (c < anl + nx) {  // core (Intep_BzIR2R_cpy_center)
-            v = row[c - anl + AL];
-        } else {  // right strip (Intep_BzIR2R_1x)
-            const T *w = bd.Wr + (size_t)(c - anl - nx) * bd.n2;
-            v = T(0);
-            for (int m = 0; m < bd.n2; m++) v += w[m] * row[bd.ox + m];
+    const int j0 = 2 * blockIdx.x, nr = min(2, g.M - j0);
+    const long long plane = (long long)(g.M + 2) * g.XP;
+    for (int e = threadIdx.x; e < 2 * L; e += blockDim.x) {
+        const int r = e >= L ? 1 : 0, i = e - r * L;
+        T v = T(0);
+        if (r < nr) {  // plane 0 of Bz is chunk-partial: add the totals of the chunks below
+            const long long o = (long long)(j0 + r + 1) * g.XP + 4 + i;
+            T p[kMaxChunks];
+#pragma unroll
+            for (int c = 1; c < kMaxChunks; c++) p[c] = c < nch ? tot[c * plane + o] : T(0);
+            v = bz[plane + o];
+#pragma unroll
+            for (int c = 1; c < kMaxChunks; c++)
+                if (c < nch) v += p[c];
         }
-        a[c] = {v, T(0)};
+        row[e] = v;
+    }
+    __syncthreads();  // the barrier is initialised, the rows are in place
+    if (!staged(bar, bd.err)) return;
+    // left strip (Intep_BzIR2R_0x), core copy (Intep_BzIR2R_cpy_center), right strip (Intep_BzIR2R_1x)
+    const T *r0 = row, *r1 = row + L;
+    if (threadIdx.x < 4) {
+        const StripPlan S = threadIdx.x < 2 ? R.s[0] : R.s[1];
+        spline_solve(tab + S.f, S.n, row + (threadIdx.x & 1) * L + S.src, 1, mbuf + threadIdx.x * R.nmax);
+    }
+    const int anl = bd.AnLx, AL = bd.AL;
+    for (int c = threadIdx.x; c < bd.Nx; c += blockDim.x) a[anl + c] = {r0[AL + c], r1[AL + c]};
+    __syncthreads();
+    const int np0 = R.s[0].npts, np = np0 + R.s[1].npts;
+    for (int e = threadIdx.x; e < np; e += blockDim.x) {
+        const int s = e >= np0 ? 1 : 0, q = e - s * np0;
+        const StripPlan S = s ? R.s[1] : R.s[0];
+        const int k0 = tabi[S.k + q];
+        const T *c = tab + S.c + q, *m0 = mbuf + 2 * s * R.nmax + k0;
+        a[S.dst + q] = {spline_out(c, S.npts, r0 + S.src + k0, 1, m0),
+                        spline_out(c, S.npts, r1 + S.src + k0, 1, m0 + R.nmax)};
     }
     __syncthreads();
-    C2<T> *res = fft_smem(a, b, bd.px, bd.twx, false);
-    C2<T> *dst = bd.FT + (size_t)j * bd.H;
-    for (int kx = threadIdx.x; kx < bd.H; kx += blockDim.x) dst[kx] = res[kx];
+    const C2<T> *Z = fft::run<false, 1>(a, b, bd.px, tw);
+    for (int kx = threadIdx.x; kx < bd.H; kx += blockDim.x) {
+        const C2<T> zk = Z[kx], zm = Z[kx == 0 ? 0 : L1 - kx];
+        C2<T> *dst = bd.FT + (size_t)kx * bd.Mp + j0;
+        dst[0] = {T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
+        if (nr == 2) dst[1] = {T(0.5) * (zk.y + zm.y), T(0.5) * (zm.x - zk.x)};
+    }
 }
 
-// ---- stage 2: y-remap in the x-frequency domain, FFT_y, filters, IFFT_y
+// ---- stage 2: y-remap in the x-frequency domain, FFT_y, the two filters and
+// both inverse FFT_y batched in one pass
 template <typename T>
-__global__ void k_cols(BoundaryDev<T> bd, StepGate gate) {
+__global__ void __launch_bounds__(kBndThreads) k_cols(BoundaryDev<T> bd, StepGate gate) {
     if (gate.base && gate.step() >= gate.nsteps) return;
-    extern __shared__ unsigned char smem_raw[];
-    const int M1 = bd.M1, M = bd.M;
-    C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw);
-    C2<T> *b = a + M1;
-    C2<T> *F = b + M1;
-    C2<T> *col = F + M1;
-    const int kx = blockIdx.x;
-    for (int m = threadIdx.x; m < M; m += blockDim.x) col[m] = bd.FT[(size_t)m * bd.H + kx];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int M1 = bd.M1, M = bd.M, kx = blockIdx.x;
+    const AxisRemap<T> &R = bd.ry;
+    const ColsLayout ly = cols_layout(bd);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + ly.bar);
+    C2<T> *tw = reinterpret_cast<C2<T> *>(smem_raw + ly.tw);
+    T *tab = reinterpret_cast<T *>(smem_raw + ly.tab);
+    int *tabi = reinterpret_cast<int *>(smem_raw + ly.tabi);
+    C2<T> *col = reinterpret_cast<C2<T> *>(smem_raw + ly.col);
+    T *gx = reinterpret_cast<T *>(smem_raw + ly.gx);
+    T *gy = reinterpret_cast<T *>(smem_raw + ly.gy);
+    C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw + ly.a);  // 2*M1
+    C2<T> *b = reinterpret_cast<C2<T> *>(smem_raw + ly.b);  // 2*M1
+    T *mbuf = reinterpret_cast<T *>(smem_raw + ly.mb);      // [strip][re/im][nmax]
+    if (threadIdx.x == 0) {
+        const unsigned btw = (unsigned)rnd16(M1 * sizeof(C2<T>)), bt = (unsigned)rnd16(R.nT * sizeof(T)),
+                       bi = (unsigned)rnd16(R.nI * sizeof(int)), bc = (unsigned)rnd16(M * sizeof(C2<T>)),
+                       bg = (unsigned)rnd16(M1 * sizeof(T));
+        mbar_init(bar, 1);
+        mbar_init_fence();
+        mbar_expect_tx(bar, btw + bt + bi + bc + 2 * bg);
+        bulk_load(tw, bd.twy, btw, bar);
+        bulk_load(tab, R.tabT, bt, bar);
+        bulk_load(tabi, R.tabI, bi, bar);
+        bulk_load(col, bd.FT + (size_t)kx * bd.Mp, bc, bar);
+        bulk_load(gx, bd.Gx + (size_t)kx * bd.M1p, bg, bar);
+        bulk_load(gy, bd.Gy + (size_t)kx * bd.M1p, bg, bar);
+    }
     __syncthreads();
-    const int any = bd.Any, ny = bd.Ny, Ay = bd.Ay;
+    if (!staged(bar, bd.err)) return;
+    // front strip (Intep_BzIR2R_0y), core copy, back strip (Intep_BzIR2R_1y); the real and
+    // imaginary parts of the column are independent lines
+    if (threadIdx.x < 4) {
+        const StripPlan S = threadIdx.x < 2 ? R.s[0] : R.s[1];
+        spline_solve(tab + S.f, S.n, reinterpret_cast<const T *>(col + S.src) + (threadIdx.x & 1), 2,
+                     mbuf + threadIdx.x * R.nmax);
+    }
+    const int any = bd.Any, Ay = bd.Ay;
+    for (int r = threadIdx.x; r < bd.Ny; r += blockDim.x) a[any + r] = col[Ay + r];
+    __syncthreads();
+    const int np0 = R.s[0].npts, np = np0 + R.s[1].npts;
+    for (int e = threadIdx.x; e < np; e += blockDim.x) {
+        const int s = e >= np0 ? 1 : 0, q = e - s * np0;
+        const StripPlan S = s ? R.s[1] : R.s[0];
+        const int k0 = tabi[S.k + q];
+        const T *c = tab + S.c + q, *m0 = mbuf + 2 * s * R.nmax + k0;
+        const T *yb = reinterpret_cast<const T *>(col + S.src + k0);
+        a[S.dst + q] = {spline_out(c, S.npts, yb, 2, m0), spline_out(c, S.npts, yb + 1, 2, m0 + R.nmax)};
+    }
+    __syncthreads();
+    C2<T> *F = fft::run<false, 1>(a, b, bd.py, tw);
+    // FBx = i*gx*F, FBy = i*gy*F (FBz_to_FBxFBy, UpContinuation_gpu.cu:113-164) side by side
+    C2<T> *in = F == a ? b : a;
     for (int r = threadIdx.x; r < M1; r += blockDim.x) {
-        C2<T> v = {T(0), T(0)};
-        if (r < any) {  // front strip (Intep_BzIR2R_0y)
-            const T *w = bd.Wf + (size_t)r * bd.n3;
-            for (int m = 0; m < bd.n3; m++) { v.x += w[m] * col[m].x; v.y += w[m] * col[m].y; }
-        } else if (r < any + ny) {
-            v = col[r - any + Ay];
-        } else {  // back strip (Intep_BzIR2R_1y)
-            const T *w = bd.Wb + (size_t)(r - any - ny) * bd.n3;
-            for (int m = 0; m < bd.n3; m++) { v.x += w[m] * col[bd.oy + m].x; v.y += w[m] * col[bd.oy + m].y; }
-        }
-        a[r] = v;
+        const C2<T> f = F[r];
+        const T ux = gx[r], uy = gy[r];
+        in[r] = {-f.y * ux, f.x * ux};
+        in[M1 + r] = {-f.y * uy, f.x * uy};
     }
     __syncthreads();
-    C2<T> *res = fft_smem(a, b, bd.py, bd.twy, false);
-    for (int r = threadIdx.x; r < M1; r += blockDim.x) F[r] = res[r];
-    __syncthreads();
-    // FBx = i*gx*F, FBy = i*gy*F (FBz_to_FBxFBy, UpContinuation_gpu.cu:113-164), then IFFT_y
-    for (int pass = 0; pass < 2; pass++) {
-        const T *gf = (pass == 0 ? bd.Gx : bd.Gy) + (size_t)kx * M1;
-        for (int r = threadIdx.x; r < M1; r += blockDim.x) {
-            C2<T> f = F[r];
-            T gv = gf[r];
-            a[r] = {-f.y * gv, f.x * gv};
-        }
-        __syncthreads();
-        C2<T> *out = fft_smem(a, b, bd.py, bd.twy, true);
-        C2<T> *dst = pass == 0 ? bd.VX : bd.VY;
-        for (int s = threadIdx.x; s < bd.S; s += blockDim.x) dst[(size_t)s * bd.H + kx] = out[bd.rows[s]];
-        __syncthreads();
+    const C2<T> *out = fft::run<true, 2>(in, F, bd.py, tw);
+    for (int s = threadIdx.x; s < bd.S; s += blockDim.x) {
+        const int rr = bd.rows[s];
+        bd.VX[(size_t)s * bd.Hp + kx] = out[rr];
+        bd.VY[(size_t)s * bd.Hp + kx] = out[M1 + rr];
     }
 }
 
 // ---- stage 3: packed inverse FFT along x of the sampled rows
 template <typename T>
-__global__ void k_rows_inv(BoundaryDev<T> bd, StepGate gate) {
+__global__ void __launch_bounds__(kBndThreads) k_rows_inv(BoundaryDev<T> bd, StepGate gate) {
     if (gate.base && gate.step() >= gate.nsteps) return;
-    extern __shared__ unsigned char smem_raw[];
-    const int L1 = bd.L1, H = bd.H;
-    C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw);
-    C2<T> *b = a + L1;
-    const int s = blockIdx.x;
-    const C2<T> *vx = bd.VX + (size_t)s * H, *vy = bd.VY + (size_t)s * H;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int L1 = bd.L1, H = bd.H, s = blockIdx.x;
+    const RowsInvLayout ly = rows_inv_layout(bd);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + ly.bar);
+    C2<T> *tw = reinterpret_cast<C2<T> *>(smem_raw + ly.tw);
+    C2<T> *vx = reinterpret_cast<C2<T> *>(smem_raw + ly.vx);
+    C2<T> *vy = reinterpret_cast<C2<T> *>(smem_raw + ly.vy);
+    C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw + ly.a);
+    C2<T> *b = reinterpret_cast<C2<T> *>(smem_raw + ly.b);
+    if (threadIdx.x == 0) {
+        const unsigned btw = (unsigned)rnd16(L1 * sizeof(C2<T>)), bv = (unsigned)rnd16(H * sizeof(C2<T>));
+        mbar_init(bar, 1);
+        mbar_init_fence();
+        mbar_expect_tx(bar, btw + 2 * bv);
+        bulk_load(tw, bd.twx, btw, bar);
+        bulk_load(vx, bd.VX + (size_t)s * bd.Hp, bv, bar);
+        bulk_load(vy, bd.VY + (size_t)s * bd.Hp, bv, bar);
+    }
+    __syncthreads();
+    if (!staged(bar, bd.err)) return;
     for (int kx = threadIdx.x; kx < H; kx += blockDim.x) {
-        C2<T> X = vx[kx], Y = vy[kx];
+        const C2<T> X = vx[kx], Y = vy[kx];
         if (kx == 0 || 2 * kx == L1) {  // self-conjugate bins carry their real parts
             a[kx] = {X.x, Y.x};
         } else {
-            a[kx] = {X.x - Y.y, X.y + Y.x};           // X + iY
-            a[L1 - kx] = {X.x + Y.y, -X.y + Y.x};     // conj(X) + i conj(Y)
+            a[kx] = {X.x - Y.y, X.y + Y.x};        // X + iY
+            a[L1 - kx] = {X.x + Y.y, -X.y + Y.x};  // conj(X) + i conj(Y)
         }
     }
     __syncthreads();
-    C2<T> *res = fft_smem(a, b, bd.px, bd.twx, true);
+    const C2<T> *res = fft::run<true, 1>(a, b, bd.px, tw);
     C2<T> *dst = bd.Z + (size_t)s * L1;
     for (int x = threadIdx.x; x < L1; x += blockDim.x) dst[x] = res[x];
 }
@@ -227,13 +343,9 @@ __global__ void k_bilinear(BoundaryDev<T> bd, T *bx, T *by, Geom g, StepGate gat
     }
 }
 
-template <typename T> static size_t smem_rows(const BoundaryDev<T> &bd, int L) {
-    return 2 * (size_t)bd.L1 * sizeof(C2<T>) + (size_t)L * sizeof(T);
-}
-template <typename T> static size_t smem_cols(const BoundaryDev<T> &bd) {
-    return (3 * (size_t)bd.M1 + bd.M) * sizeof(C2<T>);
-}
-template <typename T> static size_t smem_inv(const BoundaryDev<T> &bd) { return 2 * (size_t)bd.L1 * sizeof(C2<T>); }
+template <typename T> static size_t smem_rows(const BoundaryDev<T> &bd, int L) { return rows_fwd_layout(bd, L).total; }
+template <typename T> static size_t smem_cols(const BoundaryDev<T> &bd) { return cols_layout(bd).total; }
+template <typename T> static size_t smem_inv(const BoundaryDev<T> &bd) { return rows_inv_layout(bd).total; }
 
 template <typename T> size_t boundary_smem_need(const BoundaryDev<T> &bd, int L) {
     size_t a = smem_rows(bd, L), b = smem_cols(bd), c = smem_inv(bd);
@@ -252,43 +364,18 @@ template <typename T> cudaError_t boundary_configure(const BoundaryDev<T> &bd, i
 template <typename T>
 void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
                      StepGate gate, cudaStream_t st) {
-    k_rows_fwd<T><<<g.M, 256, smem_rows(bd, g.L), st>>>(bd, bz, tot, nch, g, gate);
-    k_cols<T><<<bd.H, 256, smem_cols(bd), st>>>(bd, gate);
-    k_rows_inv<T><<<bd.S, 256, smem_inv(bd), st>>>(bd, gate);
+    k_rows_fwd<T><<<(g.M + 1) / 2, kBndThreads, smem_rows(bd, g.L), st>>>(bd, bz, tot, nch, g, gate);
+    k_cols<T><<<bd.H, kBndThreads, smem_cols(bd), st>>>(bd, gate);
+    k_rows_inv<T><<<bd.S, kBndThreads, smem_inv(bd), st>>>(bd, gate);
     int n = (g.L + 1) * g.M + g.L * (g.M + 1);
     k_bilinear<T><<<(n + 255) / 256, 256, 0, st>>>(bd, bx, by, g, gate);
-}
-
-// stand-alone FFT of `count` rows (used by the tests through the C ABI)
-template <typename T>
-__global__ void k_fft_rows(FFTPlan P, const C2<T> *tw, const C2<T> *in, C2<T> *out, int inv) {
-    extern __shared__ unsigned char smem_raw[];
-    C2<T> *a = reinterpret_cast<C2<T> *>(smem_raw);
-    C2<T> *b = a + P.n;
-    const C2<T> *src = in + (size_t)blockIdx.x * P.n;
-    for (int x = threadIdx.x; x < P.n; x += blockDim.x) a[x] = src[x];
-    __syncthreads();
-    C2<T> *res = fft_smem(a, b, P, tw, inv != 0);
-    for (int x = threadIdx.x; x < P.n; x += blockDim.x) out[(size_t)blockIdx.x * P.n + x] = res[x];
-}
-
-template <typename T>
-cudaError_t launch_fft_rows(const FFTPlan &P, const void *tw, const void *in, void *out, int rows, int inv,
-                            cudaStream_t st) {
-    size_t sm = 2 * (size_t)P.n * sizeof(C2<T>);
-    cudaError_t e = cudaFuncSetAttribute(k_fft_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    k_fft_rows<T><<<rows, 256, sm, st>>>(P, (const C2<T> *)tw, (const C2<T> *)in, (C2<T> *)out, inv);
-    return cudaGetLastError();
 }
 
 #define INST(T)                                                                                            \
     template size_t boundary_smem_need<T>(const BoundaryDev<T> &, int);                                   \
     template cudaError_t boundary_configure<T>(const BoundaryDev<T> &, int);                              \
     template void launch_boundary<T>(const BoundaryDev<T> &, const Geom &, const T *, const T *, int, T *, T *,  \
-                                     StepGate,                                                            \
-                                     cudaStream_t);                                                       \
-    template cudaError_t launch_fft_rows<T>(const FFTPlan &, const void *, const void *, void *, int, int, cudaStream_t);
+                                     StepGate, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include "kernels.cuh"
+#include "async.cuh"
 
 namespace tcsem {
 
@@ -14,22 +15,41 @@ struct FFTPlan {
 
 template <typename T> struct C2 { T x, y; };
 
+// one strip of the spline remap in factored form (host side: SplinePlan)
+struct StripPlan {
+    int n, npts;  // source nodes, output points
+    int src, dst; // first source node in the line, first output index on the uniform line
+    int f;        // offset of the factors g, w, inv, du (n values each) in the table
+    int c;        // offset of the window weights, [6][npts]
+    int k;        // offset of the window starts in the int table
+};
+
+// the two strips of one axis, their factor/weight table and its size
+template <typename T> struct AxisRemap {
+    StripPlan s[2];
+    int nT, nI, nmax;
+    const T *tabT;
+    const int *tabI;
+};
+
 template <typename T> struct BoundaryDev {
     // plane geometry
     int L1, M1, H, M;          // H = L1/2 + 1 kept x-frequencies
-    int AnLx, Nx, AL, ox, n1, n2;
-    int Any, Ny, Ay, oy, n3;
+    int AnLx, Nx, AL;
+    int Any, Ny, Ay;
+    int Mp, M1p, Hp;           // padded strides of FT, Gx/Gy and VX/VY (16-byte rows)
     FFTPlan px, py;
     const C2<T> *twx, *twy;    // forward twiddles exp(-2 pi i k / n)
-    // spline remap weights
-    const T *Wl, *Wr, *Wf, *Wb;
-    // projected continuation filters, [H][M1], applied as i*g*F
+    // spline remaps of the x strips (left, right) and y strips (front, back)
+    AxisRemap<T> rx, ry;
+    // projected continuation filters, [H][M1p], applied as i*g*F
     const T *Gx, *Gy;
     // rows of the uniform plane that the bilinear remap samples
     int S;
     const int *rows;
     // scratch
-    C2<T> *FT, *VX, *VY, *Z;
+    C2<T> *FT, *VX, *VY, *Z;  // FT is [H][Mp]; VX, VY are [S][Hp]; Z is [S][L1]
+    int *err;                 // device error word (a bounded wait gave up)
     // bilinear tables (indices already clamped as in the reference)
     const int *bxc_II, *bxr_a, *bxr_b, *byc_II, *byr_a, *byr_b;
     const T *bxc_l, *bxr_l, *byc_l, *byr_l;
@@ -44,7 +64,4 @@ template <typename T> cudaError_t boundary_configure(const BoundaryDev<T> &bd, i
 template <typename T>
 void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
                      StepGate gate, cudaStream_t st);
-template <typename T>
-cudaError_t launch_fft_rows(const FFTPlan &P, const void *tw, const void *in, void *out, int rows, int inv,
-                            cudaStream_t st);
 }  // namespace tcsem

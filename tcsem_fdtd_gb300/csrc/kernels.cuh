@@ -97,7 +97,7 @@ struct SweepMaps {
 template <typename T>
 void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
                         const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
-                        const SourceTable<T> &src, const ZChunks &zc, int *err, cudaStream_t st);
+                        const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, int *err, cudaStream_t st);
 template <typename T> cudaError_t sweep_configure(int N);
 template <typename T> size_t sweep_smem_bytes(int N);
 int sweep_box_x();

@@ -168,27 +168,6 @@ SurveyInput read_survey_dir(const std::string &dir) {
 
 namespace {
 
-// the natural cubic spline of SplineGridConvIR2R.cu (tridiagonal rows of
-// fillA*, initialize_UpCont_gpu_resources.cu:46-144; right hand side of
-// Fill_B_*, SplineGridConvIR2R.cu:70-173), solved by elimination
-void spline_second(int n, const double *d, const double *y, double *mb) {
-    std::vector<double> dl(n), dd(n), du(n), r(n);
-    for (int i = 0; i < n; i++) {
-        if (i == 0 || i == n - 1) { dd[i] = 2.0; dl[i] = du[i] = r[i] = 0.0; continue; }
-        dd[i] = 2.0 / 3.0 * (d[i] + 0.5 * d[i - 1] + 0.5 * d[i + 1]);
-        dl[i] = 1.0 / 3.0 * (0.5 * d[i - 1] + 0.5 * d[i]);
-        du[i] = 1.0 / 3.0 * (0.5 * d[i] + 0.5 * d[i + 1]);
-        r[i] = (y[i + 1] - y[i]) / (0.5 * d[i] + 0.5 * d[i + 1]) - (y[i] - y[i - 1]) / (0.5 * d[i - 1] + 0.5 * d[i]);
-    }
-    for (int i = 1; i < n; i++) {
-        double w = dl[i] / dd[i - 1];
-        dd[i] -= w * du[i - 1];
-        r[i] -= w * r[i - 1];
-    }
-    mb[n - 1] = r[n - 1] / dd[n - 1];
-    for (int i = n - 2; i >= 0; i--) mb[i] = (r[i] - du[i] * mb[i + 1]) / dd[i];
-}
-
 // evaluation rule of Intep_BzIR2R_* (SplineGridConvIR2R.cu:180-498): cubic
 // inside the node range, the end derivative's quadratic outside it
 double spline_at(int n, const double *d, const double *xo, const double *y, const double *mb, int map, double xnew) {
@@ -212,16 +191,45 @@ double spline_at(int n, const double *d, const double *xo, const double *y, cons
     return (mb[c] * h + mc) * h + y[c];
 }
 
-// dense weights of the (linear) spline remap: W[p][m] = output p for unit input m
-void spline_weights(int n, const double *d, const double *xo, int npts, const int *map, int map_shift,
-                    const double *xnew, std::vector<double> &W) {
-    W.assign((size_t)npts * n, 0.0);
-    std::vector<double> y(n), mb(n);
-    for (int m = 0; m < n; m++) {
-        std::fill(y.begin(), y.end(), 0.0);
-        y[m] = 1.0;
-        spline_second(n, d, y.data(), mb.data());
-        for (int p = 0; p < npts; p++) W[(size_t)p * n + m] = spline_at(n, d, xo, y.data(), mb.data(), map[p] - map_shift, xnew[p]);
+// factored form of one strip remap: elimination factors of the natural cubic
+// spline system of SplineGridConvIR2R.cu (tridiagonal rows of fillA*,
+// initialize_UpCont_gpu_resources.cu:46-144; right hand side of Fill_B_*,
+// SplineGridConvIR2R.cu:70-173) and, per output point, the weights of its three-node window.  spline_at is
+// linear in (y, mb) jointly, so the window weights are its values at unit
+// vectors.
+void spline_plan(int n, const double *d, const double *xo, int npts, const int *map, int map_shift,
+                 const double *xnew, SplinePlan &P) {
+    P.n = n;
+    P.npts = npts;
+    P.g.assign(n, 0.0); P.w.assign(n, 0.0); P.inv.assign(n, 0.0); P.du.assign(n, 0.0);
+    std::vector<double> dl(n, 0.0), dd(n, 2.0), du(n, 0.0);
+    for (int i = 1; i < n - 1; i++) {
+        dd[i] = 2.0 / 3.0 * (d[i] + 0.5 * d[i - 1] + 0.5 * d[i + 1]);
+        dl[i] = 1.0 / 3.0 * (0.5 * d[i - 1] + 0.5 * d[i]);
+        du[i] = 1.0 / 3.0 * (0.5 * d[i] + 0.5 * d[i + 1]);
+    }
+    for (int i = 0; i + 1 < n; i++) P.g[i] = 1.0 / (0.5 * d[i] + 0.5 * d[i + 1]);
+    for (int i = 1; i < n; i++) {
+        P.w[i] = dl[i] / dd[i - 1];
+        dd[i] -= P.w[i] * du[i - 1];
+    }
+    for (int i = 0; i < n; i++) { P.inv[i] = 1.0 / dd[i]; P.du[i] = du[i]; }
+    P.c.assign((size_t)6 * npts, 0.0);
+    P.k0.assign(npts, 0);
+    std::vector<double> y(n, 0.0), mb(n, 0.0);
+    for (int p = 0; p < npts; p++) {
+        const int mp = map[p] - map_shift, id = std::max(mp - 1, 0);
+        if (id > n - 1) throw Error(TCSEM_ERR_INVALID, "boundary remap point beyond its strip");
+        const int k0 = std::min(std::max(id - 1, 0), n - 3);
+        P.k0[p] = k0;
+        for (int j = 0; j < 3; j++) {
+            y[k0 + j] = 1.0;
+            P.c[(size_t)j * npts + p] = spline_at(n, d, xo, y.data(), mb.data(), mp, xnew[p]);
+            y[k0 + j] = 0.0;
+            mb[k0 + j] = 1.0;
+            P.c[(size_t)(3 + j) * npts + p] = spline_at(n, d, xo, y.data(), mb.data(), mp, xnew[p]);
+            mb[k0 + j] = 0.0;
+        }
     }
 }
 
@@ -472,12 +480,12 @@ void Model::build(SurveyInput &&src) {
     n1 = AL + kNPad; n2 = I.ARx1 + I.ARx2 + kNPad; n3 = Ay + kNPad;
     ox = I.Nx + AL - kNPad; oy = I.Ny + Ay - kNPad;
     if (ox < 0 || oy < 0 || n1 > L || n3 > M) throw Error(TCSEM_ERR_INVALID, "core too small for the boundary remap");
-    spline_weights(n1, dx.data(), X.data(), AnLx_New, xBzNew2old.data(), 0, Xn.data(), Wl);
-    spline_weights(n2, dx.data() + ox, X.data() + ox, AnRx_New, xBzNew2old.data() + Nx + AnLx_New, ox,
-                   Xn.data() + Nx + AnLx_New, Wr);
-    spline_weights(n3, dy.data(), Y.data(), Any_New, yBzNew2old.data(), 0, Yn.data(), Wf);
-    spline_weights(n3, dy.data() + oy, Y.data() + oy, Any_New, yBzNew2old.data() + Ny + Any_New, oy,
-                   Yn.data() + Ny + Any_New, Wb);
+    spline_plan(n1, dx.data(), X.data(), AnLx_New, xBzNew2old.data(), 0, Xn.data(), sl);
+    spline_plan(n2, dx.data() + ox, X.data() + ox, AnRx_New, xBzNew2old.data() + Nx + AnLx_New, ox,
+                Xn.data() + Nx + AnLx_New, sr);
+    spline_plan(n3, dy.data(), Y.data(), Any_New, yBzNew2old.data(), 0, Yn.data(), sf);
+    spline_plan(n3, dy.data() + oy, Y.data() + oy, Any_New, yBzNew2old.data() + Ny + Any_New, oy,
+                Yn.data() + Ny + Any_New, sb);
 }
 
 // main.cu:212-273 plus the host decisions of EFInterp2Rx.cu:472-585

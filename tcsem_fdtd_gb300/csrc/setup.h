@@ -75,6 +75,20 @@ struct RxStencil {
     double wx[4], wy[4], wz[4];
 };
 
+// One strip of the boundary spline remap (Intep_BzIR2R_*, SplineGridConvIR2R.cu:180-498)
+// in factored form.  The natural-spline second derivatives mb of the n source
+// values y solve a fixed tridiagonal system: r_i = (y_{i+1} - y_i) g_i -
+// (y_i - y_{i-1}) g_{i-1}, forward elimination r'_i = r_i - w_i r'_{i-1}, back
+// substitution mb_i = (r'_i - du_i mb_{i+1}) inv_i, mb_0 = mb_{n-1} = 0.  Output
+// point p then reads three consecutive nodes from k0[p]:
+//   out_p = sum_j c[j][p] y_{k0+j} + c[3+j][p] mb_{k0+j}.
+struct SplinePlan {
+    int n = 0, npts = 0;
+    std::vector<double> g, w, inv, du;  // n each
+    std::vector<double> c;              // [6][npts]
+    std::vector<int> k0;                // npts
+};
+
 struct Model {
     SurveyInput in;
     int L = 0, M = 0, N = 0, AnLx_New = 0, AnRx_New = 0, Any_New = 0, L1 = 0, M1 = 0, nsrc = 0;
@@ -86,15 +100,14 @@ struct Model {
     std::vector<int> rix, riy, riz;
     std::vector<double> times, tw, dtw, wave;
 
-    // uniform-plane boundary operators
-    std::vector<double> Wl, Wr, Wf, Wb;  // spline remap weights: [AnLx_New][n1], [AnRx_New][n2], [Any_New][n3] x2
+    // uniform-plane boundary operators: the four strip remaps (left, right, front, back)
+    SplinePlan sl, sr, sf, sb;
     int n1 = 0, n2 = 0, n3 = 0, ox = 0, oy = 0;
 
     void build(SurveyInput &&in);
     Schedule schedule() const;
     std::vector<SourceSegment> sources(int itx, bool fix_dual_bipole) const;
     std::vector<RxStencil> rx_stencils(int itx) const;
-    double ref_spline_remap_check(int which, const std::vector<double> &data, int out) const;
 };
 
 // helpers shared with the tests through the C ABI

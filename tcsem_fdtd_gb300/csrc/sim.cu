@@ -1,6 +1,7 @@
 // Simulation handle and the C ABI of include/tcsem.h.
 //
-// A handle owns, on one device and one stream:
+// A handle owns, on one device and one stream (plus a high-priority side stream
+// that the steps fork onto and join back from):
 //   * two field sets (ping-pong) in the padded layout of kernels.cuh, plus the
 //     conductivity -- 13 volume arrays;
 //   * the boundary pipeline's operators and scratch (boundary.cuh);
@@ -9,7 +10,10 @@
 //   * the receiver stencils, slots and traces of the selected transmitter.
 // The step loop of main.cu:219-273 becomes: graph launch per block of
 // `graph_steps` steps, each step = boundary (4 kernels) -> fused sweep ->
-// receiver kernel, followed by one counter advance per block.
+// receiver kernel, followed by one counter advance per block.  With z-chunks
+// only the top chunk reads the air plane the boundary writes, so by default a
+// step forks: [boundary -> sweep of chunk 0] on the side stream beside [sweep
+// of chunks 1..n-1] on the main stream, joined before the receiver kernel.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -92,6 +96,7 @@ struct SimBase {
     bool begun = false;
     long step = 0;
     size_t dev_bytes = 0;
+    int launches_per_step = 0;
     virtual ~SimBase() {}
     virtual void init() = 0;
     virtual void select(int itx) = 0;
@@ -152,7 +157,7 @@ template <typename T> struct SimImpl : SimBase {
     DevMem axis_mem;
     Axis<T> ax{};
     // boundary
-    DevMem twx, twy, Wl, Wr, Wf, Wb, Gx, Gy, rows, FT, VX, VY, Zs;
+    DevMem twx, twy, remT[2], remI[2], Gx, Gy, rows, FT, VX, VY, Zs;
     DevMem bxc_II, bxr_a, bxr_b, byc_II, byr_a, byr_b, bxc_l, bxr_l, byc_l, byr_l;
     BoundaryDev<T> bd{};
     // step tables
@@ -166,8 +171,16 @@ template <typename T> struct SimImpl : SimBase {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // indexed by the starting buffer
     int gsteps = 0;
 
+    // the boundary pipeline and the top z-chunk run on `side` beside the lower chunks
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool overlap = false;
+
     ~SimImpl() override {
         for (auto &e : gexec) if (e) cudaGraphExecDestroy(e);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -220,6 +233,16 @@ template <typename T> struct SimImpl : SimBase {
         init_maps();
         init_boundary();
         init_steps();
+        // the top chunk's air plane is the only input of the sweep that the boundary writes
+        overlap = zc.n > 1 && !opts.serial_boundary;
+        if (overlap) {
+            int lo = 0, hi = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            CK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
+            CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+        }
+        launches_per_step = 4 + (overlap ? 2 : 1) + 1;
         CK(cudaStreamSynchronize(stream));
     }
 
@@ -270,12 +293,13 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaMemcpy(&h, errw.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (h) {
             CK(cudaMemset(errw.p, 0, sizeof(int)));
-            throw Error(TCSEM_ERR_CUDA, "a bounded wait in the fused sweep gave up (copy did not arrive)");
+            throw Error(TCSEM_ERR_CUDA, "a bounded wait in a kernel gave up (a bulk copy did not arrive)");
         }
     }
-    void sweep(int b, StepScalars<T> s, const StepScalars<T> *table, StepGate gate) {
+    void sweep(int b, StepScalars<T> s, const StepScalars<T> *table, StepGate gate, int c0 = 0, int c1 = -1,
+               cudaStream_t st = nullptr) {
         launch_fused_sweep<T>(maps[b], g, fs(b ^ 1), tot[b].as<T>(), tot[b ^ 1].as<T>(), ax, s, table, gate, src, zc,
-                              errw.as<int>(), stream);
+                              c0, c1 < 0 ? zc.n : c1, errw.as<int>(), st ? st : stream);
     }
     void consolidate(int b) { launch_bz_consolidate<T>(g, fs(b).bz, tot[b].as<T>(), zc, stream); }
 
@@ -283,7 +307,7 @@ template <typename T> struct SimImpl : SimBase {
         const Model &m = model;
         const int L1 = m.L1, M1 = m.M1, H = L1 / 2 + 1;
         auto tw = [&](int n, DevMem &d) {
-            std::vector<C2<T>> h(n);
+            std::vector<C2<T>> h(n + 1, C2<T>{T(0), T(0)});  // one spare entry: 16-byte bulk copies
             for (int k = 0; k < n; k++) {
                 double a = -2.0 * kPi * (double)k / (double)n;
                 h[k] = {(T)std::cos(a), (T)std::sin(a)};
@@ -292,10 +316,39 @@ template <typename T> struct SimImpl : SimBase {
         };
         tw(L1, twx);
         tw(M1, twy);
-        upload(Wl, conv(m.Wl)); upload(Wr, conv(m.Wr)); upload(Wf, conv(m.Wf)); upload(Wb, conv(m.Wb));
+        // factored spline remaps, one table per axis: per strip g, w, inv, du, then [6][npts] window weights
+        auto pack = [&](int axis, const SplinePlan &p0, const SplinePlan &p1, int src1, int dst1, AxisRemap<T> &R) {
+            std::vector<double> t;
+            std::vector<int> ti;
+            const SplinePlan *ps[2] = {&p0, &p1};
+            R.nmax = 0;
+            for (int k = 0; k < 2; k++) {
+                const SplinePlan &P = *ps[k];
+                StripPlan &S = R.s[k];
+                S.n = P.n; S.npts = P.npts;
+                S.src = k ? src1 : 0;
+                S.dst = k ? dst1 : 0;
+                S.f = (int)t.size();
+                for (const auto *v : {&P.g, &P.w, &P.inv, &P.du}) t.insert(t.end(), v->begin(), v->end());
+                S.c = (int)t.size();
+                t.insert(t.end(), P.c.begin(), P.c.end());
+                S.k = (int)ti.size();
+                ti.insert(ti.end(), P.k0.begin(), P.k0.end());
+                R.nmax = std::max(R.nmax, P.n);
+            }
+            R.nT = (int)t.size();
+            R.nI = (int)ti.size();
+            t.resize(t.size() + 4, 0.0);  // the bulk copies round up to 16 bytes
+            ti.resize(ti.size() + 4, 0);
+            upload(remT[axis], conv(t));
+            upload(remI[axis], ti);
+            R.tabT = remT[axis].as<T>();
+            R.tabI = remI[axis].as<int>();
+        };
         // continuation filters of FBz_to_FBxFBy (UpContinuation_gpu.cu:113-164) as i*g; the two
         // self-conjugate columns keep their Hermitian part so the inverse transform is real
-        std::vector<double> gx((size_t)H * M1), gy((size_t)H * M1);
+        const int M1p = (M1 + 3) & ~3;  // filter rows padded to 16 bytes
+        std::vector<double> gx((size_t)H * M1p, 0.0), gy((size_t)H * M1p, 0.0);
         const double dxm = m.in.dxmin, dym = m.in.dymin, dzm = m.in.dzmin;
         for (int kx = 0; kx < H; kx++)
             for (int ky = 0; ky < M1; ky++) {
@@ -309,17 +362,17 @@ template <typename T> struct SimImpl : SimBase {
                     a = (dxm / dym) * u1 * upcc;
                     b = (dym / dxm) * v1 * upcc;
                 }
-                gx[(size_t)kx * M1 + ky] = a;
-                gy[(size_t)kx * M1 + ky] = b;
+                gx[(size_t)kx * M1p + ky] = a;
+                gy[(size_t)kx * M1p + ky] = b;
             }
         for (int kx = 0; kx < H; kx++) {
             if (!(kx == 0 || 2 * kx == L1)) continue;
-            std::vector<double> ox(gx.begin() + (size_t)kx * M1, gx.begin() + (size_t)(kx + 1) * M1);
-            std::vector<double> oy(gy.begin() + (size_t)kx * M1, gy.begin() + (size_t)(kx + 1) * M1);
+            std::vector<double> ox(gx.begin() + (size_t)kx * M1p, gx.begin() + (size_t)kx * M1p + M1);
+            std::vector<double> oy(gy.begin() + (size_t)kx * M1p, gy.begin() + (size_t)kx * M1p + M1);
             for (int ky = 0; ky < M1; ky++) {
                 int mk = (M1 - ky) % M1;
-                gx[(size_t)kx * M1 + ky] = 0.5 * (ox[ky] - ox[mk]);
-                gy[(size_t)kx * M1 + ky] = 0.5 * (oy[ky] - oy[mk]);
+                gx[(size_t)kx * M1p + ky] = 0.5 * (ox[ky] - ox[mk]);
+                gy[(size_t)kx * M1p + ky] = 0.5 * (oy[ky] - oy[mk]);
             }
         }
         upload(Gx, conv(gx));
@@ -362,19 +415,25 @@ template <typename T> struct SimImpl : SimBase {
         upload(byc_II, hbycII); upload(byr_a, hbyra); upload(byr_b, hbyrb);
         upload(bxc_l, conv(hbxcl)); upload(bxr_l, conv(hbxrl)); upload(byc_l, conv(hbycl)); upload(byr_l, conv(hbyrl));
         const int S = (int)need.size();
-        FT.alloc((size_t)m.M * H * sizeof(C2<T>)); dev_bytes += FT.n;
-        VX.alloc((size_t)S * H * sizeof(C2<T>)); dev_bytes += VX.n;
-        VY.alloc((size_t)S * H * sizeof(C2<T>)); dev_bytes += VY.n;
+        // rows of FT and VX/VY start on 16-byte boundaries (bulk copies)
+        const int cpr = (int)(16 / sizeof(C2<T>));
+        const int Mp = (m.M + cpr - 1) / cpr * cpr, Hp = (H + cpr - 1) / cpr * cpr;
+        FT.alloc((size_t)H * Mp * sizeof(C2<T>)); dev_bytes += FT.n;
+        VX.alloc((size_t)S * Hp * sizeof(C2<T>)); dev_bytes += VX.n;
+        VY.alloc((size_t)S * Hp * sizeof(C2<T>)); dev_bytes += VY.n;
         Zs.alloc((size_t)S * L1 * sizeof(C2<T>)); dev_bytes += Zs.n;
         BoundaryDev<T> &B = bd;
         B.L1 = L1; B.M1 = M1; B.H = H; B.M = m.M;
-        B.AnLx = m.AnLx_New; B.Nx = m.in.Nx; B.AL = m.in.ALx1 + m.in.ALx2; B.ox = m.ox; B.n1 = m.n1; B.n2 = m.n2;
-        B.Any = m.Any_New; B.Ny = m.in.Ny; B.Ay = m.in.Ay1 + m.in.Ay2; B.oy = m.oy; B.n3 = m.n3;
+        B.AnLx = m.AnLx_New; B.Nx = m.in.Nx; B.AL = m.in.ALx1 + m.in.ALx2;
+        B.Any = m.Any_New; B.Ny = m.in.Ny; B.Ay = m.in.Ay1 + m.in.Ay2;
+        pack(0, m.sl, m.sr, m.ox, m.AnLx_New + m.in.Nx, B.rx);
+        pack(1, m.sf, m.sb, m.oy, m.Any_New + m.in.Ny, B.ry);
         B.px = make_plan(L1); B.py = make_plan(M1);
         B.twx = twx.as<C2<T>>(); B.twy = twy.as<C2<T>>();
-        B.Wl = Wl.as<T>(); B.Wr = Wr.as<T>(); B.Wf = Wf.as<T>(); B.Wb = Wb.as<T>();
         B.Gx = Gx.as<T>(); B.Gy = Gy.as<T>();
         B.S = S; B.rows = rows.as<int>();
+        B.Mp = Mp; B.M1p = M1p; B.Hp = Hp;
+        B.err = errw.as<int>();
         B.FT = FT.as<C2<T>>(); B.VX = VX.as<C2<T>>(); B.VY = VY.as<C2<T>>(); B.Z = Zs.as<C2<T>>();
         B.bxc_II = bxc_II.as<int>(); B.bxr_a = bxr_a.as<int>(); B.bxr_b = bxr_b.as<int>();
         B.byc_II = byc_II.as<int>(); B.byr_a = byr_a.as<int>(); B.byr_b = byr_b.as<int>();
@@ -472,8 +531,19 @@ template <typename T> struct SimImpl : SimBase {
     // one step of main.cu:219-273 on the buffers starting at `b`
     void enqueue_step(int b, StepGate gate) {
         FieldSet<T> in = fs(b), out = fs(b ^ 1);
-        launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, stream);
-        sweep(b, StepScalars<T>{}, steps.as<StepScalars<T>>(), gate);
+        const StepScalars<T> *table = steps.as<StepScalars<T>>();
+        if (overlap) {  // fork: boundary -> top chunk on `side`, chunks 1.. on `stream`; join before the receivers
+            CK(cudaEventRecord(ev_fork, stream));
+            CK(cudaStreamWaitEvent(side, ev_fork, 0));
+            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, side);
+            sweep(b, StepScalars<T>{}, table, gate, 0, 1, side);
+            sweep(b, StepScalars<T>{}, table, gate, 1, zc.n, stream);
+            CK(cudaEventRecord(ev_join, side));
+            CK(cudaStreamWaitEvent(stream, ev_join, 0));
+        } else {
+            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, stream);
+            sweep(b, StepScalars<T>{}, table, gate);
+        }
         launch_rx<T>(rd, out, tot[b ^ 1].as<T>(), zc, g, gate, RxAction{-1, 0, 0, -1, 0, 0}, stream);
     }
 
@@ -485,7 +555,7 @@ template <typename T> struct SimImpl : SimBase {
         launch_advance(gate_base.as<int>(), gsteps, stream);
         cudaError_t e = cudaStreamEndCapture(stream, &graph);
         if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&gexec[b], graph, 0);
+        e = cudaGraphInstantiateWithFlags(&gexec[b], graph, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
         return gexec[b];
@@ -765,6 +835,7 @@ tcsem_status tcsem_get_info(const tcsem_sim_t *s, tcsem_info *o) {
     o->nsteps = b.sched.nsteps;
     o->precision = b.opts.precision;
     o->device_bytes = b.dev_bytes;
+    o->launches_per_step = b.launches_per_step;
     return TCSEM_OK;
 }
 

@@ -12,6 +12,7 @@
 //    CTA recomputes the one-cell halo of E/B it needs instead of waiting for
 //    its neighbours.  Algorithmic traffic: 7 words read + 6 written per cell.
 #include "kernels.cuh"
+#include "async.cuh"
 
 namespace tcsem {
 
@@ -158,36 +159,6 @@ template <typename T> size_t smem_bytes_n(int N) {  // plus the z tables
     return ((smem_bytes<T>() + 3 * (size_t)(N + 3) * sizeof(T)) + 15) / 16 * 16;
 }
 }  // namespace fs3
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: gives up after ~1e6 polls (each poll may suspend for a while)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
-    for (int it = 0; it < (1 << 20); it++)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
 
 // reciprocal used by the E update: one MUFU op in FP32 (about 1 ulp), exact division in FP64
 template <typename T> __device__ __forceinline__ T rcp_fast(T x);
@@ -363,7 +334,8 @@ template <typename T>
 __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const __grid_constant__ SweepMaps maps, Geom g, FieldSet<T> out,
                                                       const T *__restrict__ tin, T *__restrict__ tout, Axis<T> ax,
                                                       StepScalars<T> sdir, const StepScalars<T> *__restrict__ table,
-                                                      StepGate gate, SourceTable<T> src, ZChunks zc, int *err) {
+                                                      StepGate gate, SourceTable<T> src, ZChunks zc, int cbase,
+                                                      int *err) {
     using namespace fs3;
     StepScalars<T> s = sdir;
     if (gate.base) {
@@ -392,7 +364,7 @@ __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const
     const int L = g.L, M = g.M, N = g.N, XP = g.XP;
     t.N = N;
     t.PS = (int)g.PS;
-    const int c = blockIdx.z;
+    const int c = cbase + blockIdx.z;
     t.k0 = (c * N) / zc.n;  // = zc.kb[c]
     t.k1 = ((c + 1) * N) / zc.n;
     const int ty = w < 9 ? w : lane;
@@ -433,7 +405,7 @@ __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const
 
     if (tid == 0) {
         for (int r = 0; r < RING; r++) mbar_init(t.bars + r, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init_fence();
         *t.s_flag = 0;
     }
     __syncthreads();
@@ -450,8 +422,14 @@ __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const
             const int gy = t.j0 + e / BXW, gx = t.i0 + e % BXW;  // padded coordinates
             if (gy < g.YP && gx < XP) {
                 const int pc = gy * XP + gx;
-                for (int q = c + 1; q < zc.n; q++) o += ldg(tin + q * t.PS + pc);
-                o1 = c + 1 < zc.n ? o - ldg(tin + (c + 1) * t.PS + pc) : T(0);
+                T pv[kMaxChunks];  // all loads in flight together
+#pragma unroll
+                for (int q = 1; q < kMaxChunks; q++) pv[q] = q > c && q < zc.n ? ldg(tin + q * t.PS + pc) : T(0);
+                const T first = c + 1 < zc.n ? ldg(tin + (c + 1) * t.PS + pc) : T(0);
+#pragma unroll
+                for (int q = 1; q < kMaxChunks; q++)
+                    if (q > c && q < zc.n) o += pv[q];
+                o1 = c + 1 < zc.n ? o - first : T(0);
             }
         }
         s_oc[e] = o;
@@ -518,9 +496,10 @@ __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const
 template <typename T>
 void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
                         const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
-                        const SourceTable<T> &src, const ZChunks &zc, int *err, cudaStream_t st) {
-    dim3 grd((g.L + fs3::TX - 1) / fs3::TX, (g.M + fs3::BY - 1) / fs3::BY, zc.n);
-    k_sweep<T><<<grd, fs3::NT, fs3::smem_bytes_n<T>(g.N), st>>>(maps, g, out, tin, tout, ax, s, table, gate, src, zc, err);
+                        const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, int *err, cudaStream_t st) {
+    dim3 grd((g.L + fs3::TX - 1) / fs3::TX, (g.M + fs3::BY - 1) / fs3::BY, c1 - c0);
+    k_sweep<T><<<grd, fs3::NT, fs3::smem_bytes_n<T>(g.N), st>>>(maps, g, out, tin, tout, ax, s, table, gate, src, zc,
+                                                                c0, err);
 }
 
 template <typename T> cudaError_t sweep_configure(int N) {
@@ -557,7 +536,7 @@ template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, c
     template void launch_bderivate<T>(const Geom &, FieldSet<T>, const Axis<T> &, T, cudaStream_t);                \
     template void launch_fused_sweep<T>(const SweepMaps &, const Geom &, FieldSet<T>, const T *, T *,             \
                                         const Axis<T> &, StepScalars<T>, const StepScalars<T> *, StepGate,         \
-                                        const SourceTable<T> &, const ZChunks &, int *, cudaStream_t);             \
+                                        const SourceTable<T> &, const ZChunks &, int, int, int *, cudaStream_t);             \
     template cudaError_t sweep_configure<T>(int);                                                                  \
     template size_t sweep_smem_bytes<T>(int);                                                                      \
     template void launch_bz_consolidate<T>(const Geom &, T *, T *, const ZChunks &, cudaStream_t);

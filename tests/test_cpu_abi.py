@@ -30,8 +30,37 @@ def test_opts_and_info_struct_layout_matches_header():
 
     o = Opts()
     t.library().tcsem_default_opts(C.byref(o))
-    assert o.precision == 32 and o.device == 0 and o.fix_dual_bipole == 0
+    assert o.precision == 32 and o.device == 0 and o.fix_dual_bipole == 0 and o.serial_boundary == 0
     assert C.sizeof(Opts) == 32
+
+
+def test_struct_offsets_match_the_c_compiler(tmp_path):
+    """Every field of tcsem_opts / tcsem_info sits where gcc puts it for include/tcsem.h."""
+    import shutil
+    import subprocess
+
+    from tcsem_fdtd_gb300.api import HEADER, Info, Opts
+
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    lines = []
+    for st, cname in ((Opts, "tcsem_opts"), (Info, "tcsem_info")):
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in st._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    src = tmp_path / "off.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "tcsem.h"\nint main(void) {\n' +
+                   "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "off"
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        cname, f, v = ln.split()
+        got[(cname, f)] = int(v)
+    for st, cname in ((Opts, "tcsem_opts"), (Info, "tcsem_info")):
+        assert got[(cname, "sizeof")] == C.sizeof(st), cname
+        for f, _ in st._fields_:
+            assert got[(cname, f)] == getattr(st, f).offset, (cname, f)
 
 
 def test_open_without_gpu_or_with_bad_inputs_fails_loudly(case_dir, tmp_path):
