@@ -151,7 +151,7 @@ def cpu_reference(args, d, cells):
     t0 = time.perf_counter()
     orc.run(0, max_steps=1)  # first touch of every array, and a per-step estimate
     per = time.perf_counter() - t0
-    n = int(min(30, max(2, 15.0 / max(per, 1e-6))))
+    n = int(min(2000, max(2, 15.0 / max(per, 1e-6))))  # about 15 s of CPU work
     t0 = time.perf_counter()
     _, ran = orc.run(0, max_steps=n)
     dt = time.perf_counter() - t0

@@ -8,9 +8,10 @@
  *
  * Pinning: the setup half (grid, index maps, receiver/transmitter location,
  * source waveform, sampling times) is checked bit-exactly against fixtures that
- * the reference's own host code produced (tests/golden, generated by
- * oracle/ref_host_golden.py from ModelingSetup.cpp, ModelGridMapping.cpp,
- * LoadRxTxPos.cpp, SourceWave.cpp, logspace.cpp), and Waveform() against the
+ * the reference's own host code produced (tests/golden, written by
+ * tests/golden/gen_ref_host_golden.py with the program oracle/build_ref.py
+ * compiles from ModelingSetup.cpp, ModelGridMapping.cpp, LoadRxTxPos.cpp,
+ * SourceWave.cpp, logspace.cpp), and Waveform() against the
  * reference's shipped testwaveform.dat.  The device half (E/B update, source
  * injection, spline remap, continuation, receiver interpolation) restates the
  * reference's CUDA kernels line by line; each function cites the kernel it
