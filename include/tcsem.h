@@ -126,6 +126,30 @@ tcsem_status tcsem_timed_advance(tcsem_sim_t *sim, long nsteps, double *ms);
 tcsem_status tcsem_time_steps(tcsem_sim_t *sim, int itx, long nsteps, double *ms_total, double *ms_sweep,
                               double *ms_boundary);
 
+/* tcsem_upcontinuation_noalloc: the boundary step of tcsem_upcontinuation
+ * (same kernels, same result) that allocates nothing when called.  It has no
+ * counterpart in the reference.
+ *
+ * It is meant for callers that cannot allocate device memory at the moment
+ * they run the boundary step -- a host whose memory pool already owns the
+ * device, or a step that runs while another library holds the allocator.  The
+ * four work arrays of the pipeline (x-spectra, the two filtered column sets,
+ * the packed inverse rows) are carved from one static device array of
+ * TCSEM_NOALLOC_SCRATCH_BYTES (16 MiB) built into the library, instead of the
+ * handle's own buffers.  A survey whose continuation plane needs more scratch
+ * than that (about 11.8 MB for a 736 x 736 plane over 256 rows in FP64) is
+ * refused with TCSEM_ERR_INVALID and a message giving both sizes.
+ *
+ * The first call on each device, with that device current, looks up the
+ * array's address with cudaGetSymbolAddress and keeps it; make that first call
+ * before any stream capture.  Nothing in the scratch has to start at zero:
+ * every element a call reads is written earlier in the same call.  There is
+ * one scratch per device, shared by all handles: calls that can overlap on a
+ * device (different handles, threads or streams) race on it, so the caller
+ * must serialise them. */
+#define TCSEM_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
+tcsem_status tcsem_upcontinuation_noalloc(tcsem_sim_t *sim);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,7 @@ def library():
         "tcsem_synchronize": (i, [vp]),
         "tcsem_select_tx": (i, [vp, i]),
         "tcsem_upcontinuation": (i, [vp]),
+        "tcsem_upcontinuation_noalloc": (i, [vp]),
         "tcsem_electric_field": (i, [vp, d, d, d]),
         "tcsem_bderivate": (i, [vp, d]),
         "tcsem_fused_step": (i, [vp, d, d, d, d]),
@@ -175,6 +176,10 @@ class Simulation:
 
     def upcontinuation(self):
         self._check(library().tcsem_upcontinuation(self._h))
+
+    def upcontinuation_noalloc(self):
+        """The boundary step with the library's static scratch (allocates nothing)."""
+        self._check(library().tcsem_upcontinuation_noalloc(self._h))
 
     def electric_field(self, lam, dt, wave):
         self._check(library().tcsem_electric_field(self._h, lam, dt, wave))

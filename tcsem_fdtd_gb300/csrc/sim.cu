@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -104,6 +105,7 @@ struct SimBase {
     virtual void advance(long n, int *done) = 0;
     virtual void traces(double *out) = 0;
     virtual void upcontinuation() = 0;
+    virtual void upcontinuation_in(void *scratch, size_t bytes) = 0;
     virtual void electric_field(double lam, double dt, double wave) = 0;
     virtual void bderivate(double dt) = 0;
     virtual void fused_step(double lam, double dt, double dtb, double wave) = 0;
@@ -598,6 +600,29 @@ template <typename T> struct SimImpl : SimBase {
         launch_boundary<T>(bd, g, f.bz, tot[cur].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
         CK(cudaGetLastError());
     }
+    // the same pipeline with its four work arrays carved from caller-provided scratch
+    void upcontinuation_in(void *scratch, size_t bytes) override {
+        const size_t sz[4] = {FT.n, VX.n, VY.n, Zs.n};
+        size_t off[4], need = 0;
+        for (int k = 0; k < 4; k++) {
+            off[k] = need;
+            need += (sz[k] + 255) & ~(size_t)255;
+        }
+        if (need > bytes)
+            throw Error(TCSEM_ERR_INVALID, "the continuation plane (" + std::to_string(model.L1) + " x " +
+                                               std::to_string(model.M1) + ") needs " + std::to_string(need) +
+                                               " bytes of scratch; the static scratch holds " +
+                                               std::to_string(bytes));
+        BoundaryDev<T> b2 = bd;
+        unsigned char *p = static_cast<unsigned char *>(scratch);
+        b2.FT = reinterpret_cast<C2<T> *>(p + off[0]);
+        b2.VX = reinterpret_cast<C2<T> *>(p + off[1]);
+        b2.VY = reinterpret_cast<C2<T> *>(p + off[2]);
+        b2.Z = reinterpret_cast<C2<T> *>(p + off[3]);
+        FieldSet<T> f = fs(cur);
+        launch_boundary<T>(b2, g, f.bz, tot[cur].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+        CK(cudaGetLastError());
+    }
     StepScalars<T> scal(double lam, double dt, double dtb, double wave) {
         StepScalars<T> s;
         s.lam2 = (T)(2.0 * lam); s.dt = (T)dt; s.c4 = (T)(4.0 * dt / model.mu0); s.dtb = (T)dtb; s.wave = (T)wave;
@@ -881,6 +906,30 @@ tcsem_status tcsem_write_bout(tcsem_sim_t *s, int itx, const double *t, const ch
 
 tcsem_status tcsem_select_tx(tcsem_sim_t *s, int itx) { return guard(s, [&](SimBase &b) { b.select(itx); }); }
 tcsem_status tcsem_upcontinuation(tcsem_sim_t *s) { return guard(s, [&](SimBase &b) { b.upcontinuation(); }); }
+
+// Scratch of tcsem_upcontinuation_noalloc: static device memory of the
+// library's module, one instance per device; its address is looked up once per
+// device with that device current.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[TCSEM_NOALLOC_SCRATCH_BYTES];
+
+static void *noalloc_scratch(int device) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static void *addr[kMaxDevices] = {};
+    if (device < 0 || device >= kMaxDevices) throw Error(TCSEM_ERR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        addr[device] = p;
+    }
+    return addr[device];
+}
+
+tcsem_status tcsem_upcontinuation_noalloc(tcsem_sim_t *s) {
+    return guard(s, [&](SimBase &b) { b.upcontinuation_in(noalloc_scratch(b.device), TCSEM_NOALLOC_SCRATCH_BYTES); });
+}
 tcsem_status tcsem_electric_field(tcsem_sim_t *s, double lam, double dt, double wave) {
     return guard(s, [&](SimBase &b) { b.electric_field(lam, dt, wave); });
 }
