@@ -126,6 +126,39 @@ tcsem_status tcsem_timed_advance(tcsem_sim_t *sim, long nsteps, double *ms);
 tcsem_status tcsem_time_steps(tcsem_sim_t *sim, int itx, long nsteps, double *ms_total, double *ms_sweep,
                               double *ms_boundary);
 
+/* Batches: many surveys of different sizes advanced together on one GPU, one
+ * launch per kernel per time step for all of them (no counterpart in the
+ * reference, which runs one survey per process; the batch entry points of
+ * the drop-in boundary).  A batch holds up to 64 slots; each slot is one
+ * transmitter run of one survey directory (the same four input files) with
+ * its own fields, schedule and receivers resident on the device.
+ *   tcsem_batch_create   device, precision, graph block length and z-chunks per
+ *                        slot (0 = 2) from opts;
+ *                        device_budget (bytes, 0 = no limit) bounds the sum of
+ *                        the slots' device memory
+ *   tcsem_batch_add      reads and sets up a survey; TCSEM_ERR_NOMEM (nothing
+ *                        allocated) when its estimated footprint does not fit
+ *                        the budget or the batch is full
+ *   tcsem_batch_advance  enqueues whole blocks of graph_steps steps (at least
+ *                        nsteps) for every slot still running; returns before
+ *                        they finish; slots added since the last call join here
+ *   tcsem_batch_poll     waits for the enqueued work, then lists (up to cap)
+ *                        the slots whose runs are complete; count = all of them
+ *   tcsem_batch_traces   traces [nr][NComp][Nt] of a slot (after it completed)
+ *   tcsem_batch_remove   frees a slot
+ * A batch is used from one host thread at a time. */
+typedef struct tcsem_batch tcsem_batch_t;
+tcsem_status tcsem_batch_create(const tcsem_opts *opts, size_t device_budget, tcsem_batch_t **out);
+tcsem_status tcsem_batch_destroy(tcsem_batch_t *batch);
+const char *tcsem_batch_error(const tcsem_batch_t *batch); /* last failure (batch may be NULL after a failed create) */
+tcsem_status tcsem_batch_add(tcsem_batch_t *batch, const char *dir, int itx, int *slot);
+tcsem_status tcsem_batch_advance(tcsem_batch_t *batch, long nsteps);
+tcsem_status tcsem_batch_poll(tcsem_batch_t *batch, int *slots, int cap, int *count);
+tcsem_status tcsem_batch_slot_info(tcsem_batch_t *batch, int slot, tcsem_info *info, long *steps_done);
+tcsem_status tcsem_batch_traces(tcsem_batch_t *batch, int slot, double *traces);
+tcsem_status tcsem_batch_remove(tcsem_batch_t *batch, int slot);
+tcsem_status tcsem_batch_stats(tcsem_batch_t *batch, int *slots, int *running, size_t *device_bytes);
+
 /* tcsem_upcontinuation_noalloc: the boundary step of tcsem_upcontinuation
  * (same kernels, same result) that allocates nothing when called.  It has no
  * counterpart in the reference.

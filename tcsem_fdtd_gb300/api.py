@@ -85,6 +85,18 @@ def library():
         "tcsem_time_steps": (i, [vp, i, l_, dp, dp, dp]),
         "tcsem_timed_advance": (i, [vp, l_, dp]),
     }
+    sig.update({
+        "tcsem_batch_create": (i, [C.POINTER(Opts), C.c_size_t, C.POINTER(vp)]),
+        "tcsem_batch_destroy": (i, [vp]),
+        "tcsem_batch_error": (C.c_char_p, [vp]),
+        "tcsem_batch_add": (i, [vp, C.c_char_p, i, ip]),
+        "tcsem_batch_advance": (i, [vp, l_]),
+        "tcsem_batch_poll": (i, [vp, ip, i, ip]),
+        "tcsem_batch_slot_info": (i, [vp, i, C.POINTER(Info), C.POINTER(C.c_long)]),
+        "tcsem_batch_traces": (i, [vp, i, dp]),
+        "tcsem_batch_remove": (i, [vp, i]),
+        "tcsem_batch_stats": (i, [vp, ip, ip, C.POINTER(C.c_size_t)]),
+    })
     for name, (res, args) in sig.items():
         f = getattr(L, name)
         f.restype = res
@@ -236,3 +248,78 @@ class Simulation:
         tot, sw, bn = C.c_double(), C.c_double(), C.c_double()
         self._check(library().tcsem_time_steps(self._h, itx, nsteps, C.byref(tot), C.byref(sw), C.byref(bn)))
         return tot.value, sw.value, bn.value
+
+
+class Batch:
+    """Many surveys advanced together (tcsem_batch_* of include/tcsem.h)."""
+
+    def __init__(self, precision=32, device=0, budget=0, graph_steps=0, zchunks=0):
+        L = library()
+        o = Opts()
+        L.tcsem_default_opts(C.byref(o))
+        o.precision, o.device, o.graph_steps, o.zchunks = precision, device, graph_steps, zchunks
+        h = C.c_void_p()
+        st = L.tcsem_batch_create(C.byref(o), int(budget), C.byref(h))
+        if st != 0:
+            raise TcsemError(st, L.tcsem_batch_error(None).decode())
+        self._h = h
+
+    def _check(self, st):
+        if st != 0:
+            raise TcsemError(st, library().tcsem_batch_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().tcsem_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, directory, itx=0):
+        """Set up one survey as a new slot; raises TcsemError (status 5) when it does not fit."""
+        slot = C.c_int()
+        self._check(library().tcsem_batch_add(self._h, os.fsencode(directory), itx, C.byref(slot)))
+        return slot.value
+
+    def advance(self, nsteps):
+        self._check(library().tcsem_batch_advance(self._h, nsteps))
+
+    def poll(self):
+        """Slots whose runs are complete (waits for the enqueued work)."""
+        n = C.c_int()
+        self._check(library().tcsem_batch_poll(self._h, None, 0, C.byref(n)))
+        ids = (C.c_int * max(1, n.value))()
+        self._check(library().tcsem_batch_poll(self._h, ids, n.value, C.byref(n)))
+        return list(ids[: n.value])
+
+    def info(self, slot):
+        inf, done = Info(), C.c_long()
+        self._check(library().tcsem_batch_slot_info(self._h, slot, C.byref(inf), C.byref(done)))
+        d = {f: getattr(inf, f) for f, _ in Info._fields_}
+        d["steps_done"] = done.value
+        return d
+
+    def traces(self, slot, nr=None):
+        i = self.info(slot)
+        buf = np.zeros(i["NRx"] * i["NComp"] * i["Nt"])
+        self._check(library().tcsem_batch_traces(self._h, slot, _dptr(buf)))
+        n = nr if nr is not None else i["NRx"]
+        return buf[: n * i["NComp"] * i["Nt"]].reshape(n, i["NComp"], i["Nt"])
+
+    def remove(self, slot):
+        self._check(library().tcsem_batch_remove(self._h, slot))
+
+    def stats(self):
+        n, r, b = C.c_int(), C.c_int(), C.c_size_t()
+        self._check(library().tcsem_batch_stats(self._h, C.byref(n), C.byref(r), C.byref(b)))
+        return {"slots": n.value, "running": r.value, "device_bytes": b.value}

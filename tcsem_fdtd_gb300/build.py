@@ -20,7 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libtcsem.so")
 CLI = os.path.join(PKG, "tcsem_fdtd")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["setup.cpp", "volume.cu", "boundary.cu", "rx.cu", "sim.cu"]
+SOURCES = ["setup.cpp", "volume.cu", "boundary.cu", "rx.cu", "sim.cu", "batch.cu"]
 
 
 def nvcc():

@@ -128,10 +128,8 @@ __device__ __forceinline__ bool staged(uint64_t *bar, int *err) {
 // separated in the spectrum: X1 = (Z[k] + conj Z[-k]) / 2, X2 = (Z[k] - conj Z[-k]) / 2i.
 // Output FT is stored x-frequency major, FT[kx][j].
 template <typename T>
-__global__ void __launch_bounds__(kBndThreads) k_rows_fwd(BoundaryDev<T> bd, const T *__restrict__ bz,
-                                                          const T *__restrict__ tot, int nch, Geom g,
-                                                          StepGate gate) {
-    if (gate.base && gate.step() >= gate.nsteps) return;
+__device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *__restrict__ bz,
+                                             const T *__restrict__ tot, int nch, const Geom &g, int blk) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int L1 = bd.L1, L = g.L;
     const AxisRemap<T> &R = bd.rx;
@@ -154,7 +152,7 @@ __global__ void __launch_bounds__(kBndThreads) k_rows_fwd(BoundaryDev<T> bd, con
         bulk_load(tab, R.tabT, bt, bar);
         bulk_load(tabi, R.tabI, bi, bar);
     }
-    const int j0 = 2 * blockIdx.x, nr = min(2, g.M - j0);
+    const int j0 = 2 * blk, nr = min(2, g.M - j0);
     const long long plane = (long long)(g.M + 2) * g.XP;
     for (int e = threadIdx.x; e < 2 * L; e += blockDim.x) {
         const int r = e >= L ? 1 : 0, i = e - r * L;
@@ -204,10 +202,9 @@ __global__ void __launch_bounds__(kBndThreads) k_rows_fwd(BoundaryDev<T> bd, con
 // ---- stage 2: y-remap in the x-frequency domain, FFT_y, the two filters and
 // both inverse FFT_y batched in one pass
 template <typename T>
-__global__ void __launch_bounds__(kBndThreads) k_cols(BoundaryDev<T> bd, StepGate gate) {
-    if (gate.base && gate.step() >= gate.nsteps) return;
+__device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int M1 = bd.M1, M = bd.M, kx = blockIdx.x;
+    const int M1 = bd.M1, M = bd.M, kx = blk;
     const AxisRemap<T> &R = bd.ry;
     const ColsLayout ly = cols_layout(bd);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + ly.bar);
@@ -276,10 +273,9 @@ __global__ void __launch_bounds__(kBndThreads) k_cols(BoundaryDev<T> bd, StepGat
 
 // ---- stage 3: packed inverse FFT along x of the sampled rows
 template <typename T>
-__global__ void __launch_bounds__(kBndThreads) k_rows_inv(BoundaryDev<T> bd, StepGate gate) {
-    if (gate.base && gate.step() >= gate.nsteps) return;
+__device__ __forceinline__ void rows_inv_cta(const BoundaryDev<T> &bd, int blk) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int L1 = bd.L1, H = bd.H, s = blockIdx.x;
+    const int L1 = bd.L1, H = bd.H, s = blk;
     const RowsInvLayout ly = rows_inv_layout(bd);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + ly.bar);
     C2<T> *tw = reinterpret_cast<C2<T> *>(smem_raw + ly.tw);
@@ -315,12 +311,11 @@ __global__ void __launch_bounds__(kBndThreads) k_rows_inv(BoundaryDev<T> bd, Ste
 
 // ---- stage 4: bilinear remap (Blinear_BxR2IR / Blinear_ByR2IR, UpContinuation_gpu.cu:42-110)
 template <typename T>
-__global__ void k_bilinear(BoundaryDev<T> bd, T *bx, T *by, Geom g, StepGate gate) {
-    if (gate.base && gate.step() >= gate.nsteps) return;
+__device__ __forceinline__ void bilinear_cta(const BoundaryDev<T> &bd, T *bx, T *by, const Geom &g, int blk, int nblk) {
     const int L = g.L, M = g.M;
     const int nbx = (L + 1) * M, nby = L * (M + 1);
     const T norm = bd.inv_norm;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nbx + nby; e += gridDim.x * blockDim.x) {
+    for (int e = blk * blockDim.x + threadIdx.x; e < nbx + nby; e += nblk * blockDim.x) {
         if (e < nbx) {
             const int j = e / (L + 1), i = e % (L + 1);
             const int II = bd.bxc_II[i];
@@ -343,6 +338,68 @@ __global__ void k_bilinear(BoundaryDev<T> bd, T *bx, T *by, Geom g, StepGate gat
     }
 }
 
+// ---- single-survey kernels
+template <typename T>
+__global__ void __launch_bounds__(kBndThreads) k_rows_fwd(BoundaryDev<T> bd, const T *__restrict__ bz,
+                                                          const T *__restrict__ tot, int nch, Geom g,
+                                                          StepGate gate) {
+    if (gate.base && gate.step() >= gate.nsteps) return;
+    rows_fwd_cta<T>(bd, bz, tot, nch, g, blockIdx.x);
+}
+template <typename T> __global__ void __launch_bounds__(kBndThreads) k_cols(BoundaryDev<T> bd, StepGate gate) {
+    if (gate.base && gate.step() >= gate.nsteps) return;
+    cols_cta<T>(bd, blockIdx.x);
+}
+template <typename T> __global__ void __launch_bounds__(kBndThreads) k_rows_inv(BoundaryDev<T> bd, StepGate gate) {
+    if (gate.base && gate.step() >= gate.nsteps) return;
+    rows_inv_cta<T>(bd, blockIdx.x);
+}
+template <typename T> __global__ void k_bilinear(BoundaryDev<T> bd, T *bx, T *by, Geom g, StepGate gate) {
+    if (gate.base && gate.step() >= gate.nsteps) return;
+    bilinear_cta<T>(bd, bx, by, g, blockIdx.x, gridDim.x);
+}
+
+// ---- batched kernels: block b works for slot idx.slot_of(b)
+template <typename T>
+__device__ __forceinline__ const BoundarySlot<T> *bnd_slot(const BoundarySlot<T> *slots, const BatchIndex &idx,
+                                                           int s, int &lb) {
+    const int q = idx.slot_of(blockIdx.x);
+    const BoundarySlot<T> *d = slots + q;
+    if ((long)*d->step_base + s >= d->nsteps) return nullptr;
+    lb = blockIdx.x - idx.off[q];
+    return d;
+}
+template <typename T>
+__global__ void __launch_bounds__(kBndThreads)
+    k_rows_fwd_b(const BoundarySlot<T> *__restrict__ slots, const __grid_constant__ BatchIndex idx, int s) {
+    int lb;
+    const BoundarySlot<T> *d = bnd_slot(slots, idx, s, lb);
+    if (d) rows_fwd_cta<T>(d->bd, d->bz, d->tot, d->nch, d->g, lb);
+}
+template <typename T>
+__global__ void __launch_bounds__(kBndThreads)
+    k_cols_b(const BoundarySlot<T> *__restrict__ slots, const __grid_constant__ BatchIndex idx, int s) {
+    int lb;
+    const BoundarySlot<T> *d = bnd_slot(slots, idx, s, lb);
+    if (d) cols_cta<T>(d->bd, lb);
+}
+template <typename T>
+__global__ void __launch_bounds__(kBndThreads)
+    k_rows_inv_b(const BoundarySlot<T> *__restrict__ slots, const __grid_constant__ BatchIndex idx, int s) {
+    int lb;
+    const BoundarySlot<T> *d = bnd_slot(slots, idx, s, lb);
+    if (d) rows_inv_cta<T>(d->bd, lb);
+}
+template <typename T>
+__global__ void k_bilinear_b(const BoundarySlot<T> *__restrict__ slots, const __grid_constant__ BatchIndex idx, int s) {
+    int lb;
+    const BoundarySlot<T> *d = bnd_slot(slots, idx, s, lb);
+    if (d) {
+        const int q = idx.slot_of(blockIdx.x);
+        bilinear_cta<T>(d->bd, d->bx, d->by, d->g, lb, idx.off[q + 1] - idx.off[q]);
+    }
+}
+
 template <typename T> static size_t smem_rows(const BoundaryDev<T> &bd, int L) { return rows_fwd_layout(bd, L).total; }
 template <typename T> static size_t smem_cols(const BoundaryDev<T> &bd) { return cols_layout(bd).total; }
 template <typename T> static size_t smem_inv(const BoundaryDev<T> &bd) { return rows_inv_layout(bd).total; }
@@ -361,6 +418,36 @@ template <typename T> cudaError_t boundary_configure(const BoundaryDev<T> &bd, i
     return cudaFuncSetAttribute(k_rows_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv(bd));
 }
 
+template <typename T> BoundaryBlocks boundary_blocks(const BoundaryDev<T> &bd, const Geom &g) {
+    BoundaryBlocks b;
+    b.rows_fwd = (g.M + 1) / 2;
+    b.cols = bd.H;
+    b.rows_inv = bd.S;
+    b.bilinear = ((g.L + 1) * g.M + g.L * (g.M + 1) + 255) / 256;
+    b.smem_rows = smem_rows(bd, g.L);
+    b.smem_cols = smem_cols(bd);
+    b.smem_inv = smem_inv(bd);
+    return b;
+}
+
+template <typename T> cudaError_t boundary_configure_batched(const size_t *smem) {
+    cudaError_t e;
+    e = cudaFuncSetAttribute(k_rows_fwd_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[0]);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[1]);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_inv_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[2]);
+    return e;
+}
+
+template <typename T>
+cudaError_t launch_boundary_batched(const BoundarySlot<T> *slots, const BatchIndex *idx, const size_t *smem, int s,
+                                    cudaStream_t st) {
+    if (idx[0].total()) k_rows_fwd_b<T><<<idx[0].total(), kBndThreads, smem[0], st>>>(slots, idx[0], s);
+    if (idx[1].total()) k_cols_b<T><<<idx[1].total(), kBndThreads, smem[1], st>>>(slots, idx[1], s);
+    if (idx[2].total()) k_rows_inv_b<T><<<idx[2].total(), kBndThreads, smem[2], st>>>(slots, idx[2], s);
+    if (idx[3].total()) k_bilinear_b<T><<<idx[3].total(), 256, 0, st>>>(slots, idx[3], s);
+    return cudaGetLastError();
+}
+
 template <typename T>
 void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
                      StepGate gate, cudaStream_t st) {
@@ -375,7 +462,11 @@ void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const
     template size_t boundary_smem_need<T>(const BoundaryDev<T> &, int);                                   \
     template cudaError_t boundary_configure<T>(const BoundaryDev<T> &, int);                              \
     template void launch_boundary<T>(const BoundaryDev<T> &, const Geom &, const T *, const T *, int, T *, T *,  \
-                                     StepGate, cudaStream_t);
+                                     StepGate, cudaStream_t);                                             \
+    template BoundaryBlocks boundary_blocks<T>(const BoundaryDev<T> &, const Geom &);                     \
+    template cudaError_t launch_boundary_batched<T>(const BoundarySlot<T> *, const BatchIndex *, const size_t *, int, \
+                                                    cudaStream_t);                                        \
+    template cudaError_t boundary_configure_batched<T>(const size_t *);
 INST(float)
 INST(double)
 #undef INST

@@ -56,6 +56,22 @@ template <typename T> struct BoundaryDev {
     T inv_norm;
 };
 
+// one slot of a batched boundary step (device memory)
+template <typename T> struct BoundarySlot {
+    BoundaryDev<T> bd;
+    Geom g;
+    const T *bz, *tot;  // plane 0 of Bz and the chunk totals of the current field set
+    int nch;
+    T *bx, *by;         // plane -1 of Bx/By of the current field set
+    const int *step_base;
+    long nsteps;
+};
+// blocks and dynamic shared memory of the four boundary kernels for one survey
+struct BoundaryBlocks {
+    int rows_fwd, cols, rows_inv, bilinear;
+    size_t smem_rows, smem_cols, smem_inv;
+};
+
 }  // namespace tcsem
 
 namespace tcsem {
@@ -64,4 +80,10 @@ template <typename T> cudaError_t boundary_configure(const BoundaryDev<T> &bd, i
 template <typename T>
 void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
                      StepGate gate, cudaStream_t st);
+template <typename T> BoundaryBlocks boundary_blocks(const BoundaryDev<T> &bd, const Geom &g);
+// idx[4] and smem[3]: the block lists of rows_fwd, cols, rows_inv, bilinear and the largest shared memory
+template <typename T>
+cudaError_t launch_boundary_batched(const BoundarySlot<T> *slots, const BatchIndex *idx, const size_t *smem, int s,
+                                    cudaStream_t st);
+template <typename T> cudaError_t boundary_configure_batched(const size_t *smem);
 }  // namespace tcsem

@@ -104,4 +104,45 @@ int sweep_box_x();
 int sweep_box_y();
 template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, const ZChunks &zc, cudaStream_t st);
 
+// ------------------------------------------------------------------ batches
+// Several simulations advanced by one launch per kernel: block b of a batched
+// launch belongs to slot q with off[q] <= b < off[q+1] (the list is passed by
+// value, so a block finds its slot in a few constant-cache reads).
+constexpr int kMaxSlots = 64;
+struct BatchIndex {
+    int n;                   // slots
+    int off[kMaxSlots + 1];  // first block of each slot, off[n] = total
+    __host__ __device__ int total() const { return off[n]; }
+    __device__ __forceinline__ int slot_of(int b) const {
+        int lo = 0, hi = n;  // off[lo] <= b < off[hi]; empty slots are skipped
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (off[mid] <= b) lo = mid; else hi = mid;
+        }
+        return lo;
+    }
+};
+
+// everything one step of the fused sweep needs for one slot (device memory)
+template <typename T> struct SweepSlot {
+    SweepMaps maps;
+    Geom g;
+    FieldSet<T> out;
+    const T *tin;
+    T *tout;
+    Axis<T> ax;
+    const StepScalars<T> *table;  // per step of the slot's run
+    const int *step_base;         // the slot's step counter; step = *step_base + s
+    long nsteps;
+    SourceTable<T> src;
+    ZChunks zc;
+    int *err;
+    int tiles_x, tiles_y;
+};
+// the blocks of each slot cover its chunks c0, c0+1, ... (tiles_x * tiles_y blocks per chunk)
+template <typename T>
+void launch_sweep_batched(const SweepSlot<T> *slots, const BatchIndex &idx, int s, int c0, int N_max, cudaStream_t st);
+int sweep_tiles_x(int L);
+int sweep_tiles_y(int M);
+
 }  // namespace tcsem

@@ -51,16 +51,9 @@ __device__ __forceinline__ T stencil_value(const RxDev<T> &rd, const FieldSet<T>
 }
 
 template <typename T>
-__global__ void k_rx(RxDev<T> rd, FieldSet<T> f, const T *tot, ZChunks zc, Geom g, StepGate gate, RxAction act) {
-    if (gate.base) {
-        const long st = gate.step();
-        if (st >= gate.nsteps) return;
-        const StepEntryActs &a = rd.acts[st];
-        act.e_slot = a.e_slot; act.e_first = a.e_first; act.e_count = a.e_count;
-        act.b_slot = a.b_slot; act.b_first = a.b_first; act.b_count = a.b_count;
-    }
+__device__ __forceinline__ void rx_thread(const RxDev<T> &rd, const FieldSet<T> &f, const T *tot, const ZChunks &zc,
+                                          const Geom &g, RxAction act, int idx) {
     const int nr = rd.nr, NC = rd.NComp, ne = rd.nefcmp;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= NC * nr) return;
     const int p = idx / nr, r = idx % nr;  // slot image position [p][r]
     const bool efield = p < ne;
@@ -77,9 +70,37 @@ __global__ void k_rx(RxDev<T> rd, FieldSet<T> f, const T *tot, ZChunks zc, Geom 
     }
 }
 
+template <typename T> __device__ __forceinline__ RxAction step_action(const RxDev<T> &rd, long st) {
+    const StepEntryActs &a = rd.acts[st];
+    return RxAction{a.e_slot, a.e_first, a.e_count, a.b_slot, a.b_first, a.b_count};
+}
+
+template <typename T>
+__global__ void k_rx(RxDev<T> rd, FieldSet<T> f, const T *tot, ZChunks zc, Geom g, StepGate gate, RxAction act) {
+    if (gate.base) {
+        const long st = gate.step();
+        if (st >= gate.nsteps) return;
+        act = step_action(rd, st);
+    }
+    rx_thread(rd, f, tot, zc, g, act, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <typename T>
+__global__ void k_rx_b(const RxSlot<T> *__restrict__ slots, const __grid_constant__ BatchIndex idx, int s) {
+    const int q = idx.slot_of(blockIdx.x);
+    const RxSlot<T> &d = slots[q];
+    const long st = (long)*d.step_base + s;
+    if (st >= d.nsteps) return;
+    rx_thread(d.rd, d.f, d.tot, d.zc, d.g, step_action(d.rd, st), (blockIdx.x - idx.off[q]) * blockDim.x + threadIdx.x);
+}
+
 template <typename T>
 __global__ void k_advance(int *base, int by) {
     *base += by;
+}
+
+__global__ void k_advance_all(int *counters, int n, int by) {
+    if ((int)threadIdx.x < n) counters[threadIdx.x] += by;
 }
 
 template <typename T>
@@ -87,14 +108,23 @@ void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const T *tot, const ZChunks &z
                RxAction act, cudaStream_t st) {
     int n = rd.NComp * rd.nr;
     if (n == 0) return;
-    k_rx<T><<<(n + 127) / 128, 128, 0, st>>>(rd, f, tot, zc, g, gate, act);
+    k_rx<T><<<rx_blocks(n), kRxThreads, 0, st>>>(rd, f, tot, zc, g, gate, act);
 }
 
 void launch_advance(int *base, int by, cudaStream_t st) { k_advance<float><<<1, 1, 0, st>>>(base, by); }
+void launch_advance_all(int *counters, int n, int by, cudaStream_t st) { k_advance_all<<<1, kMaxSlots, 0, st>>>(counters, n, by); }
+
+int rx_blocks(int nstencils) { return (nstencils + kRxThreads - 1) / kRxThreads; }
+
+template <typename T> void launch_rx_batched(const RxSlot<T> *slots, const BatchIndex &idx, int s, cudaStream_t st) {
+    if (idx.total()) k_rx_b<T><<<idx.total(), kRxThreads, 0, st>>>(slots, idx, s);
+}
 
 template void launch_rx<float>(const RxDev<float> &, FieldSet<float>, const float *, const ZChunks &, const Geom &,
                                StepGate, RxAction, cudaStream_t);
 template void launch_rx<double>(const RxDev<double> &, FieldSet<double>, const double *, const ZChunks &, const Geom &,
                                 StepGate, RxAction, cudaStream_t);
+template void launch_rx_batched<float>(const RxSlot<float> *, const BatchIndex &, int, cudaStream_t);
+template void launch_rx_batched<double>(const RxSlot<double> *, const BatchIndex &, int, cudaStream_t);
 
 }  // namespace tcsem

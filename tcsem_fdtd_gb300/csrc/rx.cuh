@@ -29,4 +29,19 @@ void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const T *tot, const ZChunks &z
                RxAction act, cudaStream_t st);
 void launch_advance(int *base, int by, cudaStream_t st);
 
+constexpr int kRxThreads = 128;
+int rx_blocks(int nstencils);
+// one slot of a batched receiver step (device memory)
+template <typename T> struct RxSlot {
+    RxDev<T> rd;
+    FieldSet<T> f;  // the new fields
+    const T *tot;   // their chunk totals
+    ZChunks zc;
+    Geom g;
+    const int *step_base;
+    long nsteps;
+};
+template <typename T> void launch_rx_batched(const RxSlot<T> *slots, const BatchIndex &idx, int s, cudaStream_t st);
+void launch_advance_all(int *counters, int n, int by, cudaStream_t st);
+
 }  // namespace tcsem

@@ -1,0 +1,795 @@
+#pragma once
+// Simulation state of one survey on one GPU (used by sim.cu and batch.cu).
+//
+// A handle owns, on one device and one stream (plus a high-priority side stream
+// that the steps fork onto and join back from):
+//   * two field sets (ping-pong) in the padded layout of kernels.cuh, plus the
+//     conductivity -- 13 volume arrays;
+//   * the boundary pipeline's operators and scratch (boundary.cuh);
+//   * the per-step table (scalars + receiver plan) of the whole run, so a
+//     block of steps is one CUDA graph that is captured once and replayed;
+//   * the receiver stencils, slots and traces of the selected transmitter.
+// The step loop of main.cu:219-273 becomes: graph launch per block of
+// `graph_steps` steps, each step = boundary (4 kernels) -> fused sweep ->
+// receiver kernel, followed by one counter advance per block.  With z-chunks
+// only the top chunk reads the air plane the boundary writes, so by default a
+// step forks: [boundary -> sweep of chunk 0] on the side stream beside [sweep
+// of chunks 1..n-1] on the main stream, joined before the receiver kernel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "boundary.cuh"
+#include "kernels.cuh"
+#include "rx.cuh"
+#include "setup.h"
+#include "tcsem.h"
+
+namespace tcsem {
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            throw Error(e_ == cudaErrorMemoryAllocation ? TCSEM_ERR_NOMEM : TCSEM_ERR_CUDA,             \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+    } while (0)
+
+struct DevMem {
+    void *p = nullptr;
+    size_t n = 0;
+    DevMem() = default;
+    DevMem(const DevMem &) = delete;
+    DevMem &operator=(const DevMem &) = delete;
+    ~DevMem() { if (p) cudaFree(p); }
+    void alloc(size_t bytes) {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = bytes;
+        if (bytes) CK(cudaMalloc(&p, bytes));
+    }
+    template <class U> U *as() const { return reinterpret_cast<U *>(p); }
+};
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link-time dependency on libcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+inline EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            throw Error(TCSEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+inline FFTPlan make_plan(int n) {
+    FFTPlan P{};
+    P.n = n;
+    int m = n;
+    while (m % 8 == 0) { P.radix[P.nst++] = 8; m /= 8; }
+    while (m % 4 == 0) { P.radix[P.nst++] = 4; m /= 4; }
+    while (m % 2 == 0) { P.radix[P.nst++] = 2; m /= 2; }
+    for (int p = 3; m > 1; p += 2)
+        while (m % p == 0) { P.radix[P.nst++] = p; m /= p; }
+    return P;
+}
+
+// ---------------------------------------------------------------- base class
+struct SimBase {
+    Model model;
+    Schedule sched;
+    tcsem_opts opts{};
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int itx = -1;
+    bool begun = false;
+    long step = 0;
+    size_t dev_bytes = 0;
+    int launches_per_step = 0;
+    virtual ~SimBase() {}
+    virtual void init() = 0;
+    virtual void select(int itx) = 0;
+    virtual void begin(int itx) = 0;
+    virtual void advance(long n, int *done) = 0;
+    virtual void traces(double *out) = 0;
+    virtual void upcontinuation() = 0;
+    virtual void upcontinuation_in(void *scratch, size_t bytes) = 0;
+    virtual void electric_field(double lam, double dt, double wave) = 0;
+    virtual void bderivate(double dt) = 0;
+    virtual void fused_step(double lam, double dt, double dtb, double wave) = 0;
+    virtual void rx_sample(int efield, int slot, double *values) = 0;
+    virtual void get_field(int comp, double *h) = 0;
+    virtual void set_field(int comp, const double *h) = 0;
+    virtual void time_steps(int itx, long n, double *tot, double *sweep, double *bnd) = 0;
+    virtual void timed_advance(long n, double *ms) = 0;
+    virtual void check_error() = 0;
+    size_t field_count(int comp) const {
+        size_t L = model.L, M = model.M, N = model.N;
+        switch (comp) {
+        case TCSEM_EX: return L * (M + 1) * (N + 1);
+        case TCSEM_EY: return (L + 1) * M * (N + 1);
+        case TCSEM_EZ: return (L + 1) * (M + 1) * N;
+        case TCSEM_BX: return (L + 1) * M * N;
+        case TCSEM_BY: return L * (M + 1) * N;
+        case TCSEM_BZ: return L * M * (N + 1);
+        case TCSEM_BXAIR: return (L + 1) * M;
+        case TCSEM_BYAIR: return L * (M + 1);
+        case TCSEM_CON: return L * M * N;
+        }
+        throw Error(TCSEM_ERR_INVALID, "unknown field component");
+    }
+    // extents (nx, ny, nz, z0) of a component in the reference layout
+    void extents(int comp, int &nx, int &ny, int &nz, int &z0) const {
+        int L = model.L, M = model.M, N = model.N;
+        z0 = 0;
+        switch (comp) {
+        case TCSEM_EX: nx = L; ny = M + 1; nz = N + 1; break;
+        case TCSEM_EY: nx = L + 1; ny = M; nz = N + 1; break;
+        case TCSEM_EZ: nx = L + 1; ny = M + 1; nz = N; break;
+        case TCSEM_BX: nx = L + 1; ny = M; nz = N; break;
+        case TCSEM_BY: nx = L; ny = M + 1; nz = N; break;
+        case TCSEM_BZ: nx = L; ny = M; nz = N + 1; break;
+        case TCSEM_BXAIR: nx = L + 1; ny = M; nz = 1; z0 = -1; break;
+        case TCSEM_BYAIR: nx = L; ny = M + 1; nz = 1; z0 = -1; break;
+        case TCSEM_CON: nx = L; ny = M; nz = N; break;
+        default: throw Error(TCSEM_ERR_INVALID, "unknown field component");
+        }
+    }
+};
+
+// ---------------------------------------------------------------- typed impl
+template <typename T> struct SimImpl : SimBase {
+    Geom g{};
+    DevMem fld[2][6], con, tot[2];  // two field sets + conductivity; per-set chunk totals of Bz
+    ZChunks zc{};
+    SweepMaps maps[2];              // TMA descriptors of each field set (+ conductivity)
+    DevMem errw;                    // device error word (a bounded wait gave up)
+    DevMem axis_mem;
+    Axis<T> ax{};
+    // boundary
+    DevMem twx, twy, remT[2], remI[2], Gx, Gy, rows, FT, VX, VY, Zs;
+    DevMem bxc_II, bxr_a, bxr_b, byc_II, byr_a, byr_b, bxc_l, bxr_l, byc_l, byr_l;
+    BoundaryDev<T> bd{};
+    // step tables
+    DevMem steps, acts, gate_base;
+    // transmitter dependent
+    DevMem src_coef, rx_base, rx_comp, rx_w, ef0, efs, e_l1, b_l1;
+    SourceTable<T> src{};
+    RxDev<T> rd{};
+    int cur = 0;  // buffer holding the current state
+    // graph cache
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // indexed by the starting buffer
+    int gsteps = 0;
+
+    // the boundary pipeline and the top z-chunk run on `side` beside the lower chunks
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool overlap = false;
+
+    ~SimImpl() override {
+        for (auto &e : gexec) if (e) cudaGraphExecDestroy(e);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    FieldSet<T> fs(int b) {
+        return {fld[b][0].as<T>(), fld[b][1].as<T>(), fld[b][2].as<T>(), fld[b][3].as<T>(), fld[b][4].as<T>(),
+                fld[b][5].as<T>()};
+    }
+
+    template <class U> void upload(DevMem &m, const std::vector<U> &v) {
+        m.alloc(v.size() * sizeof(U));
+        dev_bytes += m.n;
+        if (!v.empty()) CK(cudaMemcpy(m.p, v.data(), m.n, cudaMemcpyHostToDevice));
+    }
+    template <class U> std::vector<T> conv(const std::vector<U> &v) { return std::vector<T>(v.begin(), v.end()); }
+
+    void init() override {
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        const Model &m = model;
+        g = make_geom(m.L, m.M, m.N);
+        const size_t vol = (size_t)g.total() * sizeof(T);
+        for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 6; c++) {
+                fld[b][c].alloc(vol);
+                dev_bytes += vol;
+                CK(cudaMemsetAsync(fld[b][c].p, 0, vol, stream));
+            }
+        {  // conductivity in the padded layout, plane -1 (air) and padding zero
+            std::vector<T> h((size_t)g.total(), T(0));
+            for (int k = 0; k < m.N; k++)
+                for (int j = 0; j < m.M; j++)
+                    for (int i = 0; i < m.L; i++) h[g.at(i, j, k)] = (T)m.in.con[((size_t)k * m.M + j) * m.L + i];
+            upload(con, h);
+        }
+        {  // axis tables
+            std::vector<T> t;
+            auto put = [&](const std::vector<double> &v) { size_t o = t.size(); for (double x : v) t.push_back((T)x); return o; };
+            std::vector<double> rdx(m.L), rdy(m.M), rdz(m.N), rdx2(m.L, 0), rdy2(m.M, 0), rdzs(m.N);
+            for (int i = 0; i < m.L; i++) { rdx[i] = 1.0 / m.dxk[i]; if (i) rdx2[i] = 1.0 / (m.dxk[i - 1] + m.dxk[i]); }
+            for (int j = 0; j < m.M; j++) { rdy[j] = 1.0 / m.dyk[j]; if (j) rdy2[j] = 1.0 / (m.dyk[j - 1] + m.dyk[j]); }
+            for (int k = 0; k < m.N; k++) { rdz[k] = 1.0 / m.dzk[k]; rdzs[k] = k ? 1.0 / (m.dzk[k] + m.dzk[k - 1]) : 1.0 / (2.0 * m.dzk[0]); }
+            size_t o[9];
+            o[0] = put(m.dxk); o[1] = put(m.dyk); o[2] = put(m.dzk); o[3] = put(rdx); o[4] = put(rdy); o[5] = put(rdz);
+            o[6] = put(rdx2); o[7] = put(rdy2); o[8] = put(rdzs);
+            upload(axis_mem, t);
+            const T *b = axis_mem.as<T>();
+            ax = {b + o[0], b + o[1], b + o[2], b + o[3], b + o[4], b + o[5], b + o[6], b + o[7], b + o[8]};
+        }
+        init_chunks();
+        init_maps();
+        init_boundary();
+        init_steps();
+        // the top chunk's air plane is the only input of the sweep that the boundary writes
+        overlap = zc.n > 1 && !opts.serial_boundary;
+        if (overlap) {
+            int lo = 0, hi = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            CK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
+            CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+        }
+        launches_per_step = 4 + (overlap ? 2 : 1) + 1;
+        CK(cudaStreamSynchronize(stream));
+    }
+
+    // z-chunks of the fused sweep: enough CTAs to fill the GPU several times over
+    void init_chunks() {
+        const Model &m = model;
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        const long tiles = (long)((m.L + 63) / 64) * ((m.M + 7) / 8);  // 64 x 8 tiles of the fused sweep
+        int n = (int)std::min<long>(kMaxChunks, std::max<long>(1, (7L * sms + tiles - 1) / tiles));
+        n = std::min(n, std::max(1, m.N / 8));
+        if (opts.zchunks > 0) n = std::min(std::min(opts.zchunks, kMaxChunks), m.N);
+        zc.n = n;
+        for (int c = 0; c <= n; c++) zc.kb[c] = (int)(((long)c * m.N) / n);
+        const size_t tb = (size_t)n * g.PS * sizeof(T);
+        for (int b = 0; b < 2; b++) {
+            tot[b].alloc(tb);
+            dev_bytes += tb;
+            CK(cudaMemsetAsync(tot[b].p, 0, tb, stream));
+        }
+    }
+    void init_maps() {
+        if (g.total() >= (1LL << 31)) throw Error(TCSEM_ERR_INVALID, "grid too large for 32-bit offsets");
+        EncodeTiledFn enc = encode_tiled();
+        const cuuint64_t dims[3] = {(cuuint64_t)g.XP, (cuuint64_t)g.YP, (cuuint64_t)(g.N + 2)};
+        const cuuint64_t strides[2] = {(cuuint64_t)g.XP * sizeof(T), (cuuint64_t)g.PS * sizeof(T)};
+        const cuuint32_t box[3] = {(cuuint32_t)sweep_box_x(), (cuuint32_t)sweep_box_y(), 1};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const CUtensorMapDataType dt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        auto make = [&](void *ptr, CUtensorMap *m) {
+            CUresult r = enc(m, dt, 3, ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) throw Error(TCSEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        };
+        for (int b = 0; b < 2; b++) {
+            for (int a = 0; a < 6; a++) make(fld[b][a].p, &maps[b].m[a]);
+            make(con.p, &maps[b].m[6]);
+        }
+        errw.alloc(sizeof(int));
+        dev_bytes += sizeof(int);
+        CK(cudaMemset(errw.p, 0, sizeof(int)));
+        CK(sweep_configure<T>(g.N));
+    }
+    void check_error() override { check_device_error(); }
+    void check_device_error() {
+        int h = 0;
+        CK(cudaMemcpy(&h, errw.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) {
+            CK(cudaMemset(errw.p, 0, sizeof(int)));
+            throw Error(TCSEM_ERR_CUDA, "a bounded wait in a kernel gave up (a bulk copy did not arrive)");
+        }
+    }
+    void sweep(int b, StepScalars<T> s, const StepScalars<T> *table, StepGate gate, int c0 = 0, int c1 = -1,
+               cudaStream_t st = nullptr) {
+        launch_fused_sweep<T>(maps[b], g, fs(b ^ 1), tot[b].as<T>(), tot[b ^ 1].as<T>(), ax, s, table, gate, src, zc,
+                              c0, c1 < 0 ? zc.n : c1, errw.as<int>(), st ? st : stream);
+    }
+    void consolidate(int b) { launch_bz_consolidate<T>(g, fs(b).bz, tot[b].as<T>(), zc, stream); }
+
+    void init_boundary() {
+        const Model &m = model;
+        const int L1 = m.L1, M1 = m.M1, H = L1 / 2 + 1;
+        auto tw = [&](int n, DevMem &d) {
+            std::vector<C2<T>> h(n + 1, C2<T>{T(0), T(0)});  // one spare entry: 16-byte bulk copies
+            for (int k = 0; k < n; k++) {
+                double a = -2.0 * kPi * (double)k / (double)n;
+                h[k] = {(T)std::cos(a), (T)std::sin(a)};
+            }
+            upload(d, h);
+        };
+        tw(L1, twx);
+        tw(M1, twy);
+        // factored spline remaps, one table per axis: per strip g, w, inv, du, then [6][npts] window weights
+        auto pack = [&](int axis, const SplinePlan &p0, const SplinePlan &p1, int src1, int dst1, AxisRemap<T> &R) {
+            std::vector<double> t;
+            std::vector<int> ti;
+            const SplinePlan *ps[2] = {&p0, &p1};
+            R.nmax = 0;
+            for (int k = 0; k < 2; k++) {
+                const SplinePlan &P = *ps[k];
+                StripPlan &S = R.s[k];
+                S.n = P.n; S.npts = P.npts;
+                S.src = k ? src1 : 0;
+                S.dst = k ? dst1 : 0;
+                S.f = (int)t.size();
+                for (const auto *v : {&P.g, &P.w, &P.inv, &P.du}) t.insert(t.end(), v->begin(), v->end());
+                S.c = (int)t.size();
+                t.insert(t.end(), P.c.begin(), P.c.end());
+                S.k = (int)ti.size();
+                ti.insert(ti.end(), P.k0.begin(), P.k0.end());
+                R.nmax = std::max(R.nmax, P.n);
+            }
+            R.nT = (int)t.size();
+            R.nI = (int)ti.size();
+            t.resize(t.size() + 4, 0.0);  // the bulk copies round up to 16 bytes
+            ti.resize(ti.size() + 4, 0);
+            upload(remT[axis], conv(t));
+            upload(remI[axis], ti);
+            R.tabT = remT[axis].as<T>();
+            R.tabI = remI[axis].as<int>();
+        };
+        // continuation filters of FBz_to_FBxFBy (UpContinuation_gpu.cu:113-164) as i*g; the two
+        // self-conjugate columns keep their Hermitian part so the inverse transform is real
+        const int M1p = (M1 + 3) & ~3;  // filter rows padded to 16 bytes
+        std::vector<double> gx((size_t)H * M1p, 0.0), gy((size_t)H * M1p, 0.0);
+        const double dxm = m.in.dxmin, dym = m.in.dymin, dzm = m.in.dzmin;
+        for (int kx = 0; kx < H; kx++)
+            for (int ky = 0; ky < M1; ky++) {
+                double v1 = ky < M1 / 2 + 1 ? (1.0 * kPi * ky) / M1 * (dzm / dym) : -(1.0 * kPi * (M1 - ky)) / M1 * (dzm / dym);
+                double u1 = (1.0 * kPi * kx) / L1 * (dzm / dxm);
+                double a, b;
+                if (kx == 0 && ky == 0) { a = 1.0; b = 1.0; }
+                else {
+                    double w = std::sqrt(u1 * u1 + v1 * v1);
+                    double upcc = std::exp(-w) * (1.0 / w);
+                    a = (dxm / dym) * u1 * upcc;
+                    b = (dym / dxm) * v1 * upcc;
+                }
+                gx[(size_t)kx * M1p + ky] = a;
+                gy[(size_t)kx * M1p + ky] = b;
+            }
+        for (int kx = 0; kx < H; kx++) {
+            if (!(kx == 0 || 2 * kx == L1)) continue;
+            std::vector<double> ox(gx.begin() + (size_t)kx * M1p, gx.begin() + (size_t)kx * M1p + M1);
+            std::vector<double> oy(gy.begin() + (size_t)kx * M1p, gy.begin() + (size_t)kx * M1p + M1);
+            for (int ky = 0; ky < M1; ky++) {
+                int mk = (M1 - ky) % M1;
+                gx[(size_t)kx * M1p + ky] = 0.5 * (ox[ky] - ox[mk]);
+                gy[(size_t)kx * M1p + ky] = 0.5 * (oy[ky] - oy[mk]);
+            }
+        }
+        upload(Gx, conv(gx));
+        upload(Gy, conv(gy));
+        // rows of the uniform plane that the bilinear remap reads, and its tables
+        auto clampi = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi); };
+        std::vector<int> need;
+        for (int j = 0; j < m.M; j++) { int J = clampi(m.yBzold2New[j], 1, M1 - 1); need.push_back(J - 1); need.push_back(J); }
+        for (int j = 0; j <= m.M; j++) { int J = clampi(m.yoldBy2NewBz[j], 1, M1 - 1); need.push_back(J - 1); need.push_back(J); }
+        std::sort(need.begin(), need.end());
+        need.erase(std::unique(need.begin(), need.end()), need.end());
+        std::vector<int> slot(M1, -1);
+        for (size_t s = 0; s < need.size(); s++) slot[need[s]] = (int)s;
+        upload(rows, need);
+        std::vector<int> hbxcII(m.L + 1), hbxra(m.M), hbxrb(m.M), hbycII(m.L), hbyra(m.M + 1), hbyrb(m.M + 1);
+        std::vector<double> hbxcl(m.L + 1), hbxrl(m.M), hbycl(m.L), hbyrl(m.M + 1);
+        for (int i = 0; i <= m.L; i++) {
+            int II = clampi(m.xoldBx2NewBz[i], 1, L1 - 1);
+            double Xp = i == m.L ? m.X[m.L - 1] + 0.5 * m.dx[m.L - 1] : m.X[i] - 0.5 * m.dx[i];
+            hbxcII[i] = II;
+            hbxcl[i] = (Xp - m.Xn[II - 1]) / (m.Xn[II] - m.Xn[II - 1]);
+        }
+        for (int j = 0; j < m.M; j++) {
+            int J = clampi(m.yBzold2New[j], 1, M1 - 1);
+            hbxra[j] = slot[J - 1]; hbxrb[j] = slot[J];
+            hbxrl[j] = (m.Y[j] - m.Yn[J - 1]) / (m.Yn[J] - m.Yn[J - 1]);
+        }
+        for (int i = 0; i < m.L; i++) {
+            int II = clampi(m.xBzold2New[i], 1, L1 - 1);
+            hbycII[i] = II;
+            hbycl[i] = (m.X[i] - m.Xn[II - 1]) / (m.Xn[II] - m.Xn[II - 1]);
+        }
+        for (int j = 0; j <= m.M; j++) {
+            int J = clampi(m.yoldBy2NewBz[j], 1, M1 - 1);
+            double Yp = j == m.M ? m.Y[m.M - 1] + 0.5 * m.dy[m.M - 1] : m.Y[j] - 0.5 * m.dy[j];
+            hbyra[j] = slot[J - 1]; hbyrb[j] = slot[J];
+            hbyrl[j] = (Yp - m.Yn[J - 1]) / (m.Yn[J] - m.Yn[J - 1]);
+        }
+        upload(bxc_II, hbxcII); upload(bxr_a, hbxra); upload(bxr_b, hbxrb);
+        upload(byc_II, hbycII); upload(byr_a, hbyra); upload(byr_b, hbyrb);
+        upload(bxc_l, conv(hbxcl)); upload(bxr_l, conv(hbxrl)); upload(byc_l, conv(hbycl)); upload(byr_l, conv(hbyrl));
+        const int S = (int)need.size();
+        // rows of FT and VX/VY start on 16-byte boundaries (bulk copies)
+        const int cpr = (int)(16 / sizeof(C2<T>));
+        const int Mp = (m.M + cpr - 1) / cpr * cpr, Hp = (H + cpr - 1) / cpr * cpr;
+        FT.alloc((size_t)H * Mp * sizeof(C2<T>)); dev_bytes += FT.n;
+        VX.alloc((size_t)S * Hp * sizeof(C2<T>)); dev_bytes += VX.n;
+        VY.alloc((size_t)S * Hp * sizeof(C2<T>)); dev_bytes += VY.n;
+        Zs.alloc((size_t)S * L1 * sizeof(C2<T>)); dev_bytes += Zs.n;
+        BoundaryDev<T> &B = bd;
+        B.L1 = L1; B.M1 = M1; B.H = H; B.M = m.M;
+        B.AnLx = m.AnLx_New; B.Nx = m.in.Nx; B.AL = m.in.ALx1 + m.in.ALx2;
+        B.Any = m.Any_New; B.Ny = m.in.Ny; B.Ay = m.in.Ay1 + m.in.Ay2;
+        pack(0, m.sl, m.sr, m.ox, m.AnLx_New + m.in.Nx, B.rx);
+        pack(1, m.sf, m.sb, m.oy, m.Any_New + m.in.Ny, B.ry);
+        B.px = make_plan(L1); B.py = make_plan(M1);
+        B.twx = twx.as<C2<T>>(); B.twy = twy.as<C2<T>>();
+        B.Gx = Gx.as<T>(); B.Gy = Gy.as<T>();
+        B.S = S; B.rows = rows.as<int>();
+        B.Mp = Mp; B.M1p = M1p; B.Hp = Hp;
+        B.err = errw.as<int>();
+        B.FT = FT.as<C2<T>>(); B.VX = VX.as<C2<T>>(); B.VY = VY.as<C2<T>>(); B.Z = Zs.as<C2<T>>();
+        B.bxc_II = bxc_II.as<int>(); B.bxr_a = bxr_a.as<int>(); B.bxr_b = bxr_b.as<int>();
+        B.byc_II = byc_II.as<int>(); B.byr_a = byr_a.as<int>(); B.byr_b = byr_b.as<int>();
+        B.bxc_l = bxc_l.as<T>(); B.bxr_l = bxr_l.as<T>(); B.byc_l = byc_l.as<T>(); B.byr_l = byr_l.as<T>();
+        B.inv_norm = (T)(1.0 / (double)(L1 * M1));
+        size_t need_smem = boundary_smem_need(B, m.L);
+        int maxsm = 0;
+        CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+        if (need_smem > (size_t)maxsm)
+            throw Error(TCSEM_ERR_INVALID, "continuation plane too large for the shared-memory FFT (" +
+                                               std::to_string(L1) + " x " + std::to_string(M1) + ")");
+        CK(boundary_configure(B, m.L));
+    }
+
+    void init_steps() {
+        const Schedule &S = sched;
+        std::vector<StepScalars<T>> st(S.nsteps);
+        std::vector<StepEntryActs> ac(S.nsteps);
+        for (long n = 0; n < S.nsteps; n++) {
+            st[n].lam2 = (T)(2.0 * S.lam[n]);
+            st[n].dt = (T)S.dt1[n];
+            st[n].c4 = (T)(4.0 * S.dt1[n] / model.mu0);
+            st[n].dtb = (T)S.dtB[n];
+            st[n].wave = (T)S.wave[n];
+            const StepActions &a = S.act[n];
+            ac[n] = {a.e_slot, a.e_first, a.e_count, a.b_slot, a.b_first, a.b_count};
+        }
+        upload(steps, st);
+        upload(acts, ac);
+        upload(e_l1, conv(S.e_l1));
+        upload(b_l1, conv(S.b_l1));
+        gate_base.alloc(sizeof(int));
+        dev_bytes += sizeof(int);
+        gsteps = opts.graph_steps > 0 ? opts.graph_steps : 64;
+        if (gsteps % 2) gsteps++;
+    }
+
+    void select(int t) override {
+        if (t < 0 || t >= (int)model.in.tx.size()) throw Error(TCSEM_ERR_INVALID, "transmitter index out of range");
+        if (t == itx) return;
+        const Model &m = model;
+        // sources
+        std::vector<SourceSegment> segs = m.sources(t, opts.fix_dual_bipole != 0);
+        if ((int)segs.size() > kMaxSeg) throw Error(TCSEM_ERR_INVALID, "too many source segments");
+        std::vector<T> coef;
+        src = SourceTable<T>{};
+        src.nseg = (int)segs.size();
+        for (int q = 0; q < src.nseg; q++) {
+            const SourceSegment &s = segs[q];
+            src.comp[q] = s.comp; src.i[q] = s.i; src.j[q] = s.j; src.k[q] = s.k; src.count[q] = s.count;
+            src.off[q] = (int)coef.size();
+            for (double c : s.coef) coef.push_back((T)(s.gain * c));
+        }
+        upload(src_coef, coef);
+        src.coef = src_coef.as<T>();
+        // receivers
+        std::vector<RxStencil> sts = m.rx_stencils(t);
+        const int nr = m.in.tx[t].nr;
+        std::vector<long long> base(sts.size());
+        std::vector<int> comp(sts.size());
+        std::vector<T> w(sts.size() * 12);
+        for (size_t q = 0; q < sts.size(); q++) {
+            base[q] = g.at(sts[q].s1, sts[q].s2, sts[q].s3);
+            comp[q] = sts[q].comp;
+            for (int a = 0; a < 4; a++) { w[q * 12 + a] = (T)sts[q].wx[a]; w[q * 12 + 4 + a] = (T)sts[q].wy[a]; w[q * 12 + 8 + a] = (T)sts[q].wz[a]; }
+        }
+        upload(rx_base, base); upload(rx_comp, comp); upload(rx_w, w);
+        ef0.alloc((size_t)2 * m.NComp * nr * sizeof(T));
+        efs.alloc((size_t)nr * m.NComp * m.in.Nt * sizeof(T));
+        rd.nr = nr; rd.NComp = m.NComp; rd.nefcmp = m.nefcmp; rd.Nt = m.in.Nt;
+        rd.base = rx_base.as<long long>(); rd.comp = rx_comp.as<int>(); rd.w = rx_w.as<T>();
+        rd.ef0 = ef0.as<T>(); rd.efs = efs.as<T>(); rd.e_l1 = e_l1.as<T>(); rd.b_l1 = b_l1.as<T>();
+        rd.acts = acts.as<StepEntryActs>();
+        itx = t;
+        for (auto &e : gexec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+    }
+
+    void zero_state() {
+        for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 6; c++) CK(cudaMemsetAsync(fld[b][c].p, 0, fld[b][c].n, stream));
+        if (ef0.n) CK(cudaMemsetAsync(ef0.p, 0, ef0.n, stream));
+        if (efs.n) CK(cudaMemsetAsync(efs.p, 0, efs.n, stream));
+        CK(cudaMemsetAsync(gate_base.p, 0, sizeof(int), stream));
+        for (int b = 0; b < 2; b++) CK(cudaMemsetAsync(tot[b].p, 0, tot[b].n, stream));
+        cur = 0;
+        step = 0;
+    }
+
+    void begin(int t) override {
+        select(t);
+        zero_state();
+        begun = true;
+    }
+
+    // one step of main.cu:219-273 on the buffers starting at `b`
+    void enqueue_step(int b, StepGate gate) {
+        FieldSet<T> in = fs(b), out = fs(b ^ 1);
+        const StepScalars<T> *table = steps.as<StepScalars<T>>();
+        if (overlap) {  // fork: boundary -> top chunk on `side`, chunks 1.. on `stream`; join before the receivers
+            CK(cudaEventRecord(ev_fork, stream));
+            CK(cudaStreamWaitEvent(side, ev_fork, 0));
+            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, side);
+            sweep(b, StepScalars<T>{}, table, gate, 0, 1, side);
+            sweep(b, StepScalars<T>{}, table, gate, 1, zc.n, stream);
+            CK(cudaEventRecord(ev_join, side));
+            CK(cudaStreamWaitEvent(stream, ev_join, 0));
+        } else {
+            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, stream);
+            sweep(b, StepScalars<T>{}, table, gate);
+        }
+        launch_rx<T>(rd, out, tot[b ^ 1].as<T>(), zc, g, gate, RxAction{-1, 0, 0, -1, 0, 0}, stream);
+    }
+
+    cudaGraphExec_t graph_for(int b) {
+        if (gexec[b]) return gexec[b];
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int s = 0; s < gsteps; s++) enqueue_step(b ^ (s & 1), StepGate{gate_base.as<int>(), s, sched.nsteps});
+        launch_advance(gate_base.as<int>(), gsteps, stream);
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiateWithFlags(&gexec[b], graph, cudaGraphInstantiateFlagUseNodePriority);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        return gexec[b];
+    }
+
+    void advance(long n, int *done) override {
+        if (!begun) throw Error(TCSEM_ERR_STATE, "tcsem_begin must precede tcsem_advance");
+        long todo = std::min(sched.nsteps - step, std::max(0L, n));
+        // whole captured blocks (an even number of steps returns the state to `cur`)
+        while (todo >= gsteps) {
+            CK(cudaGraphLaunch(graph_for(cur), stream));
+            step += gsteps;
+            todo -= gsteps;
+        }
+        // remainder: the same kernels launched one by one, gated on the same counter
+        if (todo > 0) {
+            for (long q = 0; q < todo; q++)
+                enqueue_step(cur ^ (int)(q & 1), StepGate{gate_base.as<int>(), (int)q, sched.nsteps});
+            launch_advance(gate_base.as<int>(), (int)todo, stream);
+            if (todo & 1) cur ^= 1;
+            step += todo;
+        }
+        CK(cudaGetLastError());
+        if (done) *done = step >= sched.nsteps;
+    }
+
+    void traces(double *out) override {
+        CK(cudaStreamSynchronize(stream));
+        check_device_error();
+        std::vector<T> h(efs.n / sizeof(T));
+        CK(cudaMemcpy(h.data(), efs.p, efs.n, cudaMemcpyDeviceToHost));
+        bool finite = true;
+        for (size_t q = 0; q < h.size(); q++) { out[q] = (double)h[q]; finite &= std::isfinite(out[q]); }
+        if (!finite) throw Error(TCSEM_ERR_NUMERIC, "non-finite receiver samples");
+    }
+
+    // ---- batches: the descriptors of one step that reads field set b and writes b ^ 1
+    void batch_slot(int b, const int *counter, SweepSlot<T> &sw, BoundarySlot<T> &bs, RxSlot<T> &rs) {
+        FieldSet<T> in = fs(b), out = fs(b ^ 1);
+        sw.maps = maps[b]; sw.g = g; sw.out = out; sw.tin = tot[b].as<T>(); sw.tout = tot[b ^ 1].as<T>();
+        sw.ax = ax; sw.table = steps.as<StepScalars<T>>(); sw.step_base = counter; sw.nsteps = sched.nsteps;
+        sw.src = src; sw.zc = zc; sw.err = errw.as<int>();
+        sw.tiles_x = sweep_tiles_x(g.L); sw.tiles_y = sweep_tiles_y(g.M);
+        bs.bd = bd; bs.g = g; bs.bz = in.bz; bs.tot = tot[b].as<T>(); bs.nch = zc.n; bs.bx = in.bx; bs.by = in.by;
+        bs.step_base = counter; bs.nsteps = sched.nsteps;
+        rs.rd = rd; rs.f = out; rs.tot = tot[b ^ 1].as<T>(); rs.zc = zc; rs.g = g;
+        rs.step_base = counter; rs.nsteps = sched.nsteps;
+    }
+    int sweep_blocks() const { return sweep_tiles_x(g.L) * sweep_tiles_y(g.M) * zc.n; }
+    int rx_stencils() const { return rd.NComp * rd.nr; }
+    // an upper bound of the device memory init() allocates, from the host model alone
+    static size_t estimate_bytes(const Model &m, long nsteps) {
+        const Geom gg = make_geom(m.L, m.M, m.N);
+        const size_t vol = (size_t)gg.total() * sizeof(T), H = m.L1 / 2 + 2, L1 = m.L1, M1 = m.M1;
+        size_t b = 13 * vol + 2 * (size_t)kMaxChunks * gg.PS * sizeof(T);
+        b += (H * (m.M + 2) + 2 * M1 * H + M1 * L1) * 2 * sizeof(T) + 2 * H * (M1 + 4) * sizeof(T);
+        b += (size_t)nsteps * (sizeof(StepScalars<T>) + sizeof(StepEntryActs)) + ((size_t)4 << 20);
+        return b;
+    }
+
+    // ---- per-stage seam
+    void upcontinuation() override {
+        FieldSet<T> f = fs(cur);
+        launch_boundary<T>(bd, g, f.bz, tot[cur].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+        CK(cudaGetLastError());
+    }
+    // the same pipeline with its four work arrays carved from caller-provided scratch
+    void upcontinuation_in(void *scratch, size_t bytes) override {
+        const size_t sz[4] = {FT.n, VX.n, VY.n, Zs.n};
+        size_t off[4], need = 0;
+        for (int k = 0; k < 4; k++) {
+            off[k] = need;
+            need += (sz[k] + 255) & ~(size_t)255;
+        }
+        if (need > bytes)
+            throw Error(TCSEM_ERR_INVALID, "the continuation plane (" + std::to_string(model.L1) + " x " +
+                                               std::to_string(model.M1) + ") needs " + std::to_string(need) +
+                                               " bytes of scratch; the static scratch holds " +
+                                               std::to_string(bytes));
+        BoundaryDev<T> b2 = bd;
+        unsigned char *p = static_cast<unsigned char *>(scratch);
+        b2.FT = reinterpret_cast<C2<T> *>(p + off[0]);
+        b2.VX = reinterpret_cast<C2<T> *>(p + off[1]);
+        b2.VY = reinterpret_cast<C2<T> *>(p + off[2]);
+        b2.Z = reinterpret_cast<C2<T> *>(p + off[3]);
+        FieldSet<T> f = fs(cur);
+        launch_boundary<T>(b2, g, f.bz, tot[cur].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+        CK(cudaGetLastError());
+    }
+    StepScalars<T> scal(double lam, double dt, double dtb, double wave) {
+        StepScalars<T> s;
+        s.lam2 = (T)(2.0 * lam); s.dt = (T)dt; s.c4 = (T)(4.0 * dt / model.mu0); s.dtb = (T)dtb; s.wave = (T)wave;
+        return s;
+    }
+    void need_tx() { if (itx < 0) select(0); }
+    void electric_field(double lam, double dt, double wave) override {
+        need_tx();
+        consolidate(cur);
+        launch_update_e<T>(g, fs(cur), con.as<T>(), ax, scal(lam, dt, 0, wave), src, stream);
+        CK(cudaGetLastError());
+    }
+    void bderivate(double dtb) override {
+        consolidate(cur);
+        launch_bderivate<T>(g, fs(cur), ax, (T)dtb, stream);
+        CK(cudaGetLastError());
+    }
+    void fused_step(double lam, double dt, double dtb, double wave) override {
+        need_tx();
+        // the sweep writes every updated cell of the other buffer; the air plane must follow the state
+        T *dst_bx = fs(cur ^ 1).bx, *dst_by = fs(cur ^ 1).by;
+        sweep(cur, scal(lam, dt, dtb, wave), nullptr, StepGate{nullptr, 0, 0});
+        CK(cudaMemcpyAsync(dst_bx, fs(cur).bx, g.PS * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(dst_by, fs(cur).by, g.PS * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaGetLastError());
+        cur ^= 1;
+    }
+    void rx_sample(int efield, int slot, double *values) override {
+        need_tx();
+        if (slot < 0 || slot > 1) throw Error(TCSEM_ERR_INVALID, "slot must be 0 or 1");
+        RxAction a{-1, 0, 0, -1, 0, 0};
+        if (efield) a.e_slot = slot; else a.b_slot = slot;
+        launch_rx<T>(rd, fs(cur), tot[cur].as<T>(), zc, g, StepGate{nullptr, 0, 0}, a, stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(stream));
+        size_t n = (size_t)model.NComp * rd.nr;
+        std::vector<T> h(n);
+        CK(cudaMemcpy(h.data(), ef0.as<T>() + (size_t)slot * n, n * sizeof(T), cudaMemcpyDeviceToHost));
+        for (size_t q = 0; q < n; q++) values[q] = (double)h[q];
+    }
+
+    // ---- field access in the reference layout
+    DevMem &field_mem(int comp, int b) {
+        if (comp == TCSEM_CON) return con;
+        if (comp == TCSEM_BXAIR) return fld[b][3];
+        if (comp == TCSEM_BYAIR) return fld[b][4];
+        return fld[b][comp];
+    }
+    void get_field(int comp, double *h) override {
+        int nx, ny, nz, z0;
+        extents(comp, nx, ny, nz, z0);
+        if (comp == TCSEM_BZ) consolidate(cur);
+        CK(cudaStreamSynchronize(stream));
+        DevMem &dm = field_mem(comp, cur);
+        std::vector<T> buf((size_t)g.total());
+        CK(cudaMemcpy(buf.data(), dm.p, buf.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        size_t q = 0;
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) h[q++] = (double)buf[g.at(i, j, k + z0)];
+    }
+    void set_field(int comp, const double *h) override {
+        int nx, ny, nz, z0;
+        extents(comp, nx, ny, nz, z0);
+        CK(cudaStreamSynchronize(stream));
+        DevMem &dm = field_mem(comp, cur);
+        std::vector<T> buf((size_t)g.total());
+        CK(cudaMemcpy(buf.data(), dm.p, buf.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        size_t q = 0;
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) buf[g.at(i, j, k + z0)] = (T)h[q++];
+        CK(cudaMemcpy(dm.p, buf.data(), buf.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (comp != TCSEM_CON) {  // keep the other buffer consistent for the fused sweep's untouched cells
+            DevMem &other = field_mem(comp, cur ^ 1);
+            CK(cudaMemcpy(other.p, buf.data(), buf.size() * sizeof(T), cudaMemcpyHostToDevice));
+        }
+        if (comp == TCSEM_BZ)  // a plain Bz plane: no chunk offsets
+            for (int b = 0; b < 2; b++) CK(cudaMemset(tot[b].p, 0, tot[b].n));
+    }
+
+    void timed_advance(long n, double *ms_out) override {
+        if (!begun) throw Error(TCSEM_ERR_STATE, "tcsem_begin must precede tcsem_timed_advance");
+        graph_for(cur);  // capture (once) outside the timed region
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaStreamSynchronize(stream));
+        CK(cudaEventRecord(e0, stream));
+        advance(n, nullptr);
+        CK(cudaEventRecord(e1, stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (ms_out) *ms_out = ms;
+    }
+
+    void time_steps(int t, long n, double *ms_tot, double *ms_sweep, double *bnd) override {
+        begin(t);
+        n = std::min(n, sched.nsteps);
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        graph_for(cur);  // capture outside the timed region
+        graph_for(cur ^ 1);
+        CK(cudaStreamSynchronize(stream));
+        CK(cudaEventRecord(e0, stream));
+        advance(n, nullptr);
+        CK(cudaEventRecord(e1, stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms_tot) *ms_tot = ms;
+        const int reps = 20;
+        if (ms_sweep) {
+            StepScalars<T> s = scal(sched.lam[0], sched.dt1[0], sched.dtB[0], 0.0);
+            CK(cudaEventRecord(e0, stream));
+            for (int r = 0; r < reps; r++)
+                sweep(r & 1, s, nullptr, StepGate{nullptr, 0, 0});
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            *ms_sweep = ms / reps;
+        }
+        if (bnd) {
+            CK(cudaEventRecord(e0, stream));
+            for (int r = 0; r < reps; r++) {
+                FieldSet<T> f = fs(r & 1);
+                launch_boundary<T>(bd, g, f.bz, tot[r & 1].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream);
+            }
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            *bnd = ms / reps;
+        }
+        CK(cudaGetLastError());
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        begun = false;
+    }
+};
+
+}  // namespace tcsem

@@ -330,19 +330,13 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
     return true;
 }
 
+// one CTA of the sweep: tile (bx, by) of z-chunk c with the step scalars s
 template <typename T>
-__global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const __grid_constant__ SweepMaps maps, Geom g, FieldSet<T> out,
-                                                      const T *__restrict__ tin, T *__restrict__ tout, Axis<T> ax,
-                                                      StepScalars<T> sdir, const StepScalars<T> *__restrict__ table,
-                                                      StepGate gate, SourceTable<T> src, ZChunks zc, int cbase,
-                                                      int *err) {
+__device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, const FieldSet<T> &out,
+                                          const T *__restrict__ tin, T *__restrict__ tout, const Axis<T> &ax,
+                                          StepScalars<T> s, const SourceTable<T> &src, const ZChunks &zc, int bx,
+                                          int by, int c, int *err) {
     using namespace fs3;
-    StepScalars<T> s = sdir;
-    if (gate.base) {
-        const long st = gate.step();
-        if (st >= gate.nsteps) return;
-        s = table[st];
-    }
     constexpr int BS = boxs<T>();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SweepThread<T> t;
@@ -359,12 +353,11 @@ __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     t.tid = tid;
-    t.i0 = blockIdx.x * TX;
-    t.j0 = blockIdx.y * BY;
+    t.i0 = bx * TX;
+    t.j0 = by * BY;
     const int L = g.L, M = g.M, N = g.N, XP = g.XP;
     t.N = N;
     t.PS = (int)g.PS;
-    const int c = cbase + blockIdx.z;
     t.k0 = (c * N) / zc.n;  // = zc.kb[c]
     t.k1 = ((c + 1) * N) / zc.n;
     const int ty = w < 9 ? w : lane;
@@ -494,6 +487,33 @@ __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1) k_sweep(const
 }
 
 template <typename T>
+__global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1)
+    k_sweep(const __grid_constant__ SweepMaps maps, Geom g, FieldSet<T> out, const T *__restrict__ tin,
+            T *__restrict__ tout, Axis<T> ax, StepScalars<T> sdir, const StepScalars<T> *__restrict__ table,
+            StepGate gate, SourceTable<T> src, ZChunks zc, int cbase, int *err) {
+    StepScalars<T> s = sdir;
+    if (gate.base) {
+        const long st = gate.step();
+        if (st >= gate.nsteps) return;
+        s = table[st];
+    }
+    sweep_cta<T>(maps, g, out, tin, tout, ax, s, src, zc, blockIdx.x, blockIdx.y, cbase + blockIdx.z, err);
+}
+
+// every slot of a batch in one launch: block b belongs to the slot whose range of idx holds it
+template <typename T>
+__global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1)
+    k_sweep_batched(const SweepSlot<T> *__restrict__ slots, const __grid_constant__ BatchIndex idx, int s, int c0) {
+    const int q = idx.slot_of(blockIdx.x);
+    const SweepSlot<T> &d = slots[q];
+    const long st = (long)*d.step_base + s;
+    if (st >= d.nsteps) return;
+    const int lb = blockIdx.x - idx.off[q];
+    const int bx = lb % d.tiles_x, rest = lb / d.tiles_x, by = rest % d.tiles_y, c = c0 + rest / d.tiles_y;
+    sweep_cta<T>(d.maps, d.g, d.out, d.tin, d.tout, d.ax, d.table[st], d.src, d.zc, bx, by, c, d.err);
+}
+
+template <typename T>
 void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
                         const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
                         const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, int *err, cudaStream_t st) {
@@ -502,8 +522,19 @@ void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, c
                                                                 c0, err);
 }
 
+template <typename T>
+void launch_sweep_batched(const SweepSlot<T> *slots, const BatchIndex &idx, int s, int c0, int N_max, cudaStream_t st) {
+    if (idx.total() == 0) return;
+    k_sweep_batched<T><<<idx.total(), fs3::NT, fs3::smem_bytes_n<T>(N_max), st>>>(slots, idx, s, c0);
+}
+int sweep_tiles_x(int L) { return (L + fs3::TX - 1) / fs3::TX; }
+int sweep_tiles_y(int M) { return (M + fs3::BY - 1) / fs3::BY; }
+
 template <typename T> cudaError_t sweep_configure(int N) {
-    return cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs3::smem_bytes_n<T>(N));
+    const int sm = (int)fs3::smem_bytes_n<T>(N);
+    cudaError_t e = cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_sweep_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
 }
 template <typename T> size_t sweep_smem_bytes(int N) { return fs3::smem_bytes_n<T>(N); }
 int sweep_box_x() { return fs3::BXW; }
@@ -539,7 +570,8 @@ template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, c
                                         const SourceTable<T> &, const ZChunks &, int, int, int *, cudaStream_t);             \
     template cudaError_t sweep_configure<T>(int);                                                                  \
     template size_t sweep_smem_bytes<T>(int);                                                                      \
-    template void launch_bz_consolidate<T>(const Geom &, T *, T *, const ZChunks &, cudaStream_t);
+    template void launch_bz_consolidate<T>(const Geom &, T *, T *, const ZChunks &, cudaStream_t);             \
+    template void launch_sweep_batched<T>(const SweepSlot<T> *, const BatchIndex &, int, int, int, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

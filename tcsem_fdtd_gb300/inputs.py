@@ -183,6 +183,19 @@ def conductivity(c, g=None):
         rng = np.random.default_rng(m.get("seed", 0))
         lo, hi = m.get("range", (0.1, 4.0))
         return np.exp(rng.uniform(np.log(lo), np.log(hi), size=(N, M, L)))
+    if kind == "layered":  # horizontal layers [(z_top, sigma), ...] below z = 0, plus blocks
+        con = np.empty((N, M, L))
+        zc = Zc[:, None, None] * np.ones((1, M, L))
+        con[:] = m["layers"][0][1]
+        for (ztop, s) in m["layers"]:
+            con[zc >= ztop] = s
+        for b in m.get("blocks", []):
+            xs, ys, zs, s = b
+            sel = ((Xc[None, None, :] >= xs[0]) & (Xc[None, None, :] < xs[1]) &
+                   (Yc[None, :, None] >= ys[0]) & (Yc[None, :, None] < ys[1]) &
+                   (Zc[:, None, None] >= zs[0]) & (Zc[:, None, None] < zs[1]))
+            con[sel] = s
+        return con
     if kind == "marine":
         con = np.empty((N, M, L))
         zc = Zc[:, None, None] * np.ones((1, M, L))
@@ -283,6 +296,38 @@ CASES = {
         transmitters=[dict(ort=1, len=50.0, x=0.0, y=0.0, z=950.0)],
     ),
 }
+
+
+def batch_case(seed, size=((96, 192), (96, 192), (96, 128)), tn=(1.0,)):
+    """One survey of the batched workload, drawn from ``seed``.
+
+    Grid uniform in [96, 192] x [96, 192] x [96, 128] cells at 25 m (20-cell
+    boundary strips growing by 1.08 on each lateral side and at the bottom),
+    a background of 1-3 horizontal layers with resistivities 0.3-5 ohm-m, a
+    20-200 ohm-m resistive block, an x-directed transmitter placed along a line
+    through the core, 40 inline receivers, time window 1e-3 s to one of `tn`.
+    """
+    rng = np.random.default_rng(seed)
+    L, M, N = (int(rng.integers(a, b + 1)) for a, b in size)
+    strip, dmin = 20, 25.0
+    nx, ny, nz = L - 2 * strip, M - 2 * strip, N - strip
+    half_x, depth = 0.5 * nx * dmin, nz * dmin
+    nl = int(rng.integers(1, 4))
+    tops = [0.0] + sorted(float(z) for z in rng.uniform(0.15 * depth, 0.8 * depth, nl - 1))
+    layers = [(z, 1.0 / float(rng.uniform(0.3, 5.0))) for z in tops]
+    bx = float(rng.uniform(0.15, 0.35)) * 2 * half_x
+    bz0 = float(rng.uniform(0.4, 0.7)) * depth
+    block = ((-0.5 * bx, 0.5 * bx), (-0.5 * bx, 0.5 * bx), (bz0, bz0 + 4 * dmin), 1.0 / float(rng.uniform(20.0, 200.0)))
+    ztx = round(0.3 * depth / dmin) * dmin + 0.5 * dmin
+    xtx = float(rng.uniform(-0.5, 0.5)) * half_x
+    xr = np.linspace(-0.8 * half_x, 0.8 * half_x, 40)
+    return _base(
+        dmin=(dmin, dmin, dmin), arg1=1.08, arg2=1.08, xsplit=(0, strip, nx, strip, 0), ysplit=(0, strip, ny),
+        zsplit=(0, strip, nz), n1=200, sita_t=1e-4, sfa1=2.0, sfa2=2.0, T0=1e-3, Tn=float(rng.choice(tn)), Nt=41,
+        comps=(1, 1, 0, 1, 1, 1), model=dict(kind="layered", layers=layers, blocks=[block]),
+        receivers=[(float(x), 0.0, ztx + dmin) for x in xr],
+        transmitters=[dict(ort=1, len=2 * dmin, x=xtx, y=0.0, z=ztx)],
+    )
 
 
 def case(name, **overrides):

@@ -1,0 +1,98 @@
+"""Batched form: several surveys of different sizes advanced together.
+
+Each slot's traces must equal the same survey run alone through
+tcsem_run with the same z-chunk count (two, the batch default; the batched
+launches run the same per-CTA code on the same data): the check allows
+1e-12 (FP64) / 1e-6 (FP32) relative to each trace's peak.
+Slots join while others run and leave when done; admission respects the
+device-memory budget.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {64: 1e-12, 32: 1e-6}
+
+
+def rel_err(got, exp):
+    peak = np.abs(exp).max(axis=2, keepdims=True)
+    return float((np.abs(got - exp) / np.where(peak > 0, peak, 1.0)).max())
+
+
+@pytest.fixture(scope="module")
+def built():
+    from tcsem_fdtd_gb300 import build
+
+    build.build()
+    return True
+
+
+def alone(d, precision, itx=0):
+    from tcsem_fdtd_gb300 import Simulation
+
+    with Simulation(d, precision=precision, zchunks=2) as sim:
+        return sim.run(itx)
+
+
+def run_to_end(b, block=64, limit=100000):
+    done = set()
+    for _ in range(limit):
+        if b.stats()["running"] == 0:
+            break
+        b.advance(block)
+        done.update(b.poll())
+    return done
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_batch_equals_each_survey_alone(built, case_dir, precision):
+    from tcsem_fdtd_gb300 import Batch
+
+    cases = [("tiny", 0), ("small", 0), ("txvar", 3), ("cfg1", 0)]
+    dirs = [(case_dir(n), itx) for n, itx in cases]
+    with Batch(precision=precision) as b:
+        slots = [b.add(d, itx) for d, itx in dirs]
+        st = b.stats()
+        assert st["slots"] == 4 and st["running"] == 4 and st["device_bytes"] > 0
+        done = run_to_end(b)
+        assert done == set(slots)
+        for (d, itx), s in zip(dirs, slots):
+            info = b.info(s)
+            assert info["steps_done"] == info["nsteps"]
+            exp = alone(d, precision, itx)
+            got = b.traces(s, nr=exp.shape[0])
+            assert np.all(np.isfinite(got))
+            assert rel_err(got, exp) <= TOL[precision], (d, itx)
+
+
+def test_slots_join_and_leave_between_blocks(built, case_dir):
+    """A survey that joins while another runs, and one that leaves early, give the same traces."""
+    from tcsem_fdtd_gb300 import Batch
+
+    d1, d2, d3 = case_dir("small"), case_dir("tiny"), case_dir("txvar")
+    with Batch(precision=32, graph_steps=32) as b:
+        s1 = b.add(d1)
+        s3 = b.add(d3, 1)
+        b.advance(96)  # three blocks of s1 and s3 alone
+        s2 = b.add(d2)  # joins at the next block
+        b.advance(64)
+        b.remove(s3)  # leaves before its run ends
+        done = run_to_end(b, block=32)
+        assert {s1, s2} <= done
+        for d, s in ((d1, s1), (d2, s2)):
+            exp = alone(d, 32)
+            assert rel_err(b.traces(s, nr=exp.shape[0]), exp) <= TOL[32]
+        b.remove(s1)
+        b.remove(s2)
+        assert b.stats()["slots"] == 0
+
+
+def test_admission_by_device_budget(built, case_dir):
+    from tcsem_fdtd_gb300 import Batch, TcsemError
+
+    with Batch(precision=32, budget=1 << 20) as b:  # 1 MiB: not even the tiny survey fits
+        with pytest.raises(TcsemError) as e:
+            b.add(case_dir("tiny"))
+        assert e.value.status == 5 and "budget" in str(e.value)
+        assert b.stats()["slots"] == 0
