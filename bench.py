@@ -10,6 +10,10 @@ input formats).  With N > 1 (torchrun) every rank runs an independent replica
 on its own GPU; the time is the maximum over ranks and the value the sum of
 cells*steps over ranks.
 
+--workload cfg4 runs 64 generated surveys as one device batch and one at a
+time (simulations per hour); --workload cfg5 serves a seeded Poisson stream of
+requests with continuous batching and one at a time (sims/hr, p50/p99).
+
 --impl reference times the CPU implementation of the same path (the FP64 C
 restatement in oracle/, all host threads) on the same workload, on a bounded
 number of steps, rank 0 only.
@@ -194,6 +198,70 @@ def run_reference_arm(args, dist):
     return 0
 
 
+def run_batch_workloads(args, dist):
+    """cfg4: generated surveys advanced as one device batch vs one at a time (sims/hr).
+    cfg5: a seeded Poisson stream of requests served with continuous batching (sims/hr, p50/p99)."""
+    from tcsem_fdtd_gb300 import Batch, Simulation, build, inputs
+    from tcsem_fdtd_gb300 import serve as sv
+
+    build.build()
+    if args.workload == "cfg5":
+        reqs = sv.make_stream(args.surveys, args.rate, 5 + dist.rank, tn=(1.0, 10.0))
+        srv = sv.Server(budget=64 << 30, block=64)
+        try:
+            batched = sv.summary(reqs, sv.serve(reqs, srv))
+        finally:
+            srv.close()
+        plain_reqs = [sv.Request(r.rid, r.directory, r.arrival) for r in reqs]
+        plain = sv.summary(plain_reqs, sv.run_plain(plain_reqs))
+        line = {"metric": "sims/hr", "value": dist.reduce(batched["sims_per_hour"], "sum"), "unit": "sims/hr",
+                "n_gpus": dist.world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic", "impl": "gb300",
+                "config": {"workload": "cfg5", "requests": args.surveys, "rate_per_s": args.rate,
+                           "sizes": "64x64x48 .. 256x256x160", "windows_s": [1.0, 10.0], "budget_gb": 64},
+                "batched": batched, "plain": plain, "vs_plain": batched["sims_per_hour"] / plain["sims_per_hour"]}
+        if dist.rank == 0:
+            print(json.dumps(line), flush=True)
+        return 0
+    root = tempfile.mkdtemp(prefix="tcsem_bench_cfg4_")
+    dirs = []
+    for q in range(args.surveys):
+        d = os.path.join(root, f"s{q:03d}")
+        inputs.write_case(inputs.batch_case(1000 * dist.rank + q), d)
+        dirs.append(d)
+    cells_steps = 0
+    t0 = time.perf_counter()
+    for d in dirs:  # one at a time: open, all steps, traces
+        with Simulation(d, precision=args.precision, device=dist.local) as sim:
+            sim.run(0)
+            i = sim.info
+            cells_steps += i["L"] * i["M"] * i["N"] * i["nsteps"]
+    tp = time.perf_counter() - t0
+    dist.barrier()
+    t0 = time.perf_counter()
+    with Batch(precision=args.precision, device=dist.local) as b:
+        slots = [b.add(d) for d in dirs]
+        while b.stats()["running"]:
+            b.advance(256)
+        b.poll()
+        for s in slots:
+            b.traces(s)
+    tb = time.perf_counter() - t0
+    tb_max = dist.reduce(tb, "max")
+    n_all = dist.reduce(len(dirs), "sum")
+    line = {"metric": "sims/hr", "value": 3600.0 * n_all / tb_max, "unit": "sims/hr", "n_gpus": dist.world,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic", "impl": "gb300",
+            "config": {"workload": "cfg4", "surveys": len(dirs), "grids": "96..192 x 96..192 x 96..128",
+                       "window_s": 1.0, "what": "tcsem_batch_add of every survey, all steps, traces to host"},
+            "batched_s": tb, "plain_s": tp, "plain_sims_per_hour": 3600.0 * len(dirs) / tp,
+            "vs_plain": tp / tb,
+            "Gcell_steps_per_s": {"batched": cells_steps / tb / 1e9, "plain": cells_steps / tp / 1e9}}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -203,12 +271,16 @@ def main():
     ap.add_argument("--workload", default="cfg3")
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--surveys", type=int, default=64, help="cfg4: surveys in the batch; cfg5: requests")
+    ap.add_argument("--rate", type=float, default=8.0, help="cfg5: mean request arrivals per second")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     dist = Dist()
     try:
         if args.impl == "reference":
             return run_reference_arm(args, dist)
+        if args.workload in ("cfg4", "cfg5"):
+            return run_batch_workloads(args, dist)
         return run_gb300(args, dist)
     finally:
         dist.close()

@@ -145,6 +145,7 @@ tcsem_status tcsem_time_steps(tcsem_sim_t *sim, int itx, long nsteps, double *ms
  *   tcsem_batch_poll     waits for the enqueued work, then lists (up to cap)
  *                        the slots whose runs are complete; count = all of them
  *   tcsem_batch_traces   traces [nr][NComp][Nt] of a slot (after it completed)
+ *   tcsem_batch_write_bout  the slot's Tx<k>.bout (format of main.cu:280-292)
  *   tcsem_batch_remove   frees a slot
  * A batch is used from one host thread at a time. */
 typedef struct tcsem_batch tcsem_batch_t;
@@ -156,6 +157,7 @@ tcsem_status tcsem_batch_advance(tcsem_batch_t *batch, long nsteps);
 tcsem_status tcsem_batch_poll(tcsem_batch_t *batch, int *slots, int cap, int *count);
 tcsem_status tcsem_batch_slot_info(tcsem_batch_t *batch, int slot, tcsem_info *info, long *steps_done);
 tcsem_status tcsem_batch_traces(tcsem_batch_t *batch, int slot, double *traces);
+tcsem_status tcsem_batch_write_bout(tcsem_batch_t *batch, int slot, const char *path);
 tcsem_status tcsem_batch_remove(tcsem_batch_t *batch, int slot);
 tcsem_status tcsem_batch_stats(tcsem_batch_t *batch, int *slots, int *running, size_t *device_bytes);
 

@@ -95,6 +95,7 @@ def library():
         "tcsem_batch_slot_info": (i, [vp, i, C.POINTER(Info), C.POINTER(C.c_long)]),
         "tcsem_batch_traces": (i, [vp, i, dp]),
         "tcsem_batch_remove": (i, [vp, i]),
+        "tcsem_batch_write_bout": (i, [vp, i, C.c_char_p]),
         "tcsem_batch_stats": (i, [vp, ip, ip, C.POINTER(C.c_size_t)]),
     })
     for name, (res, args) in sig.items():
@@ -315,6 +316,9 @@ class Batch:
         self._check(library().tcsem_batch_traces(self._h, slot, _dptr(buf)))
         n = nr if nr is not None else i["NRx"]
         return buf[: n * i["NComp"] * i["Nt"]].reshape(n, i["NComp"], i["Nt"])
+
+    def write_bout(self, slot, path):
+        self._check(library().tcsem_batch_write_bout(self._h, slot, os.fsencode(path)))
 
     def remove(self, slot):
         self._check(library().tcsem_batch_remove(self._h, slot))

@@ -31,6 +31,7 @@ struct BatchBase {
     virtual int poll(int *ids, int cap) = 0;
     virtual void slot_info(int id, tcsem_info *info, long *steps_done) = 0;
     virtual void traces(int id, double *out) = 0;
+    virtual void write_bout(int id, const char *path) = 0;
     virtual void remove(int id) = 0;
     virtual void stats(int *slots, int *running, size_t *bytes) = 0;
 };
@@ -242,6 +243,14 @@ template <typename T> struct BatchImpl : BatchBase {
         s.sim->traces(out);
     }
 
+    void write_bout(int id, const char *path) override {
+        Slot &s = find(id);
+        const Model &m = s.sim->model;
+        std::vector<double> t((size_t)m.in.rx.size() * m.NComp * m.in.Nt);
+        traces(id, t.data());
+        write_bout_file(m, s.sim->itx, t.data(), path);
+    }
+
     void remove(int id) override {
         CK(cudaStreamSynchronize(stream));
         for (size_t q = 0; q < slots.size(); q++)
@@ -362,6 +371,11 @@ tcsem_status tcsem_batch_slot_info(tcsem_batch_t *b, int slot, tcsem_info *info,
 tcsem_status tcsem_batch_traces(tcsem_batch_t *b, int slot, double *traces) {
     if (!traces) return TCSEM_ERR_INVALID;
     return bguard(b, [&](BatchBase &x) { x.traces(slot, traces); });
+}
+
+tcsem_status tcsem_batch_write_bout(tcsem_batch_t *b, int slot, const char *path) {
+    if (!path) return TCSEM_ERR_INVALID;
+    return bguard(b, [&](BatchBase &x) { x.write_bout(slot, path); });
 }
 
 tcsem_status tcsem_batch_remove(tcsem_batch_t *b, int slot) {

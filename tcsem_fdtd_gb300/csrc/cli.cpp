@@ -2,7 +2,8 @@
 // Reads FDTD_setup.in, Cond.bin, Receiver.in and Transmitter.in from the
 // working directory (or the directory given as the first argument), runs every
 // transmitter and writes Tx<k>.bout and testwaveform.dat like main.cu:58-324.
-// Options: --fp64 (double-precision build mode), --device N, --fix-dual-bipole.
+// Options: --fp64 (double-precision build mode), --device N, --fix-dual-bipole,
+// --batch (all transmitters advanced together as one device batch).
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -16,12 +17,17 @@ int main(int argc, char **argv) {
     std::string dir = ".";
     tcsem_opts o;
     tcsem_default_opts(&o);
+    bool batch = false;
     for (int a = 1; a < argc; a++) {
         if (!std::strcmp(argv[a], "--fp64")) o.precision = TCSEM_FP64;
+        else if (!std::strcmp(argv[a], "--batch")) batch = true;
         else if (!std::strcmp(argv[a], "--fix-dual-bipole")) o.fix_dual_bipole = 1;
         else if (!std::strcmp(argv[a], "--device") && a + 1 < argc) o.device = std::atoi(argv[++a]);
         else if (argv[a][0] != '-') dir = argv[a];
-        else { std::fprintf(stderr, "usage: tcsem_fdtd [dir] [--fp64] [--device N] [--fix-dual-bipole]\n"); return 2; }
+        else {
+            std::fprintf(stderr, "usage: tcsem_fdtd [dir] [--fp64] [--device N] [--fix-dual-bipole] [--batch]\n");
+            return 2;
+        }
     }
     auto t0 = std::chrono::steady_clock::now();
     tcsem_sim_t *sim = nullptr;
@@ -51,6 +57,49 @@ int main(int argc, char **argv) {
     }
     auto tg = std::chrono::steady_clock::now();
     int rc = 0;
+    if (batch) {  // every transmitter as one slot of a device batch
+        tcsem_close(sim);
+        tcsem_batch_t *b = nullptr;
+        if (tcsem_batch_create(&o, 0, &b) != TCSEM_OK) {
+            std::fprintf(stderr, "Error: %s\n", tcsem_batch_error(nullptr));
+            return 1;
+        }
+        std::vector<int> slots(info.NTx, -1);
+        for (int itx = 0; itx < info.NTx; itx++) {
+            std::printf("start to model the EM field generated by Tx %d\n", itx + 1);
+            if (tcsem_batch_add(b, dir.c_str(), itx, &slots[itx]) != TCSEM_OK) {
+                std::fprintf(stderr, "Error in transmitter %d: %s\n", itx + 1, tcsem_batch_error(b));
+                slots[itx] = -1;
+                rc = 1;
+            }
+        }
+        int running = 0;
+        do {
+            if (tcsem_batch_advance(b, 1024) != TCSEM_OK) {
+                std::fprintf(stderr, "Error: %s\n", tcsem_batch_error(b));
+                rc = 1;
+                break;
+            }
+            tcsem_batch_stats(b, nullptr, &running, nullptr);
+        } while (running > 0);
+        int nd = 0;
+        tcsem_batch_poll(b, nullptr, 0, &nd);
+        for (int itx = 0; itx < info.NTx; itx++) {
+            if (slots[itx] < 0) continue;
+            char name[64];
+            std::snprintf(name, sizeof name, "/Tx%d.bout", itx + 1);
+            if (tcsem_batch_write_bout(b, slots[itx], (dir + name).c_str()) != TCSEM_OK) {
+                std::fprintf(stderr, "Error writing %s: %s\n", name + 1, tcsem_batch_error(b));
+                rc = 1;
+            }
+            std::printf("end of time iteration for Tx %d\n", itx + 1);
+        }
+        tcsem_batch_destroy(b);
+        auto t1 = std::chrono::steady_clock::now();
+        std::printf("FDTD modleing completed, runtime=%8.1f sec.\n", std::chrono::duration<double>(t1 - t0).count());
+        std::printf("Pure GPU runtime=%8.1f sec.\n", std::chrono::duration<double>(t1 - tg).count());
+        return rc;
+    }
     // traces of one transmitter fit in NRx*NComp*Nt doubles
     std::vector<double> traces((size_t)info.NRx * info.NComp * info.Nt);
     for (int itx = 0; itx < info.NTx; itx++) {

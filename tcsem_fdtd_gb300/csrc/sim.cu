@@ -127,15 +127,7 @@ tcsem_status tcsem_run(tcsem_sim_t *s, int itx, double *t) {
 tcsem_status tcsem_write_bout(tcsem_sim_t *s, int itx, const double *t, const char *path) {
     return guard(s, [&](SimBase &b) {
         if (!t || !path) throw Error(TCSEM_ERR_INVALID, "null argument");
-        if (itx < 0 || itx >= (int)b.model.in.tx.size()) throw Error(TCSEM_ERR_INVALID, "transmitter index out of range");
-        // main.cu:280-292: int32 nr, NComp, Nt then float64 [nr][NComp][Nt]
-        int hdr[3] = {b.model.in.tx[itx].nr, b.model.NComp, b.model.in.Nt};
-        FILE *f = std::fopen(path, "wb");
-        if (!f) throw Error(TCSEM_ERR_IO, std::string("cannot write ") + path);
-        size_t n = (size_t)hdr[0] * hdr[1] * hdr[2];
-        bool ok = std::fwrite(hdr, sizeof(int), 3, f) == 3 && std::fwrite(t, sizeof(double), n, f) == n;
-        ok &= std::fclose(f) == 0;
-        if (!ok) throw Error(TCSEM_ERR_IO, std::string("short write to ") + path);
+        write_bout_file(b.model, itx, t, path);
     });
 }
 

@@ -86,6 +86,18 @@ inline FFTPlan make_plan(int n) {
     return P;
 }
 
+// Tx<k>.bout of main.cu:280-292: int32 nr, NComp, Nt then float64 [nr][NComp][Nt]
+inline void write_bout_file(const Model &m, int itx, const double *t, const char *path) {
+    if (itx < 0 || itx >= (int)m.in.tx.size()) throw Error(TCSEM_ERR_INVALID, "transmitter index out of range");
+    int hdr[3] = {m.in.tx[itx].nr, m.NComp, m.in.Nt};
+    FILE *f = std::fopen(path, "wb");
+    if (!f) throw Error(TCSEM_ERR_IO, std::string("cannot write ") + path);
+    size_t n = (size_t)hdr[0] * hdr[1] * hdr[2];
+    bool ok = std::fwrite(hdr, sizeof(int), 3, f) == 3 && std::fwrite(t, sizeof(double), n, f) == n;
+    ok &= std::fclose(f) == 0;
+    if (!ok) throw Error(TCSEM_ERR_IO, std::string("short write to ") + path);
+}
+
 // ---------------------------------------------------------------- base class
 struct SimBase {
     Model model;

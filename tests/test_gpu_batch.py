@@ -96,3 +96,28 @@ def test_admission_by_device_budget(built, case_dir):
             b.add(case_dir("tiny"))
         assert e.value.status == 5 and "budget" in str(e.value)
         assert b.stats()["slots"] == 0
+
+
+def test_cli_batch_mode_writes_the_same_files(built, case_dir, tmp_path):
+    """tcsem_fdtd --batch (all transmitters as one batch) writes the same Tx<k>.bout as the serial CLI."""
+    import shutil
+    import subprocess
+
+    from tcsem_fdtd_gb300 import build
+
+    out = {}
+    for mode in ("serial", "batch"):
+        d = tmp_path / mode
+        shutil.copytree(case_dir("txvar"), d)
+        args = [build.CLI, str(d)] + (["--batch"] if mode == "batch" else [])
+        r = subprocess.run(args, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out[mode] = {}
+        for k in range(1, 7):
+            raw = open(d / f"Tx{k}.bout", "rb").read()
+            hdr = tuple(int(v) for v in np.frombuffer(raw[:12], np.int32))
+            out[mode][k] = (hdr, np.frombuffer(raw[12:], np.float64).reshape(hdr))
+    for k in range(1, 7):
+        (h1, a), (h2, b) = out["serial"][k], out["batch"][k]
+        assert h1 == h2
+        assert rel_err(b, a) <= 1e-4  # FP32; two z-chunks per batch slot vs the single-survey default
