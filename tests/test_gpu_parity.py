@@ -92,7 +92,7 @@ def test_bderivate_stage(built, case_dir, name, precision):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-@pytest.mark.parametrize("name", ["tiny", "small", "cfg1"])
+@pytest.mark.parametrize("name", ["tiny", "small", "cfg1", "cfg2", "cfg3"])  # planes up to 832 x 180 and 736 x 736
 def test_upcontinuation_stage(built, case_dir, name, precision):
     sim, orc = pair(case_dir, name, precision)
     randomize(sim, orc, 11, names=("Bz",))
