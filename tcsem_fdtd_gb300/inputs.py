@@ -275,6 +275,16 @@ CASES = {
         receivers=[(500.0 + 250.0 * i, 0.0, 0.0) for i in range(15)],
         transmitters=[dict(ort=1, len=25.0, x=0.0, y=0.0, z=0.0)],
     ),
+    # uniform 1 S/m half-space fine enough for the closed-form check: 12.5 m core
+    # cells, growth 1.2, x-directed 25 m wire at the surface, inline receivers
+    # at 250-1000 m on the surface
+    "halfspace": _base(
+        dmin=(12.5, 12.5, 12.5), arg1=1.2, arg2=1.2, xsplit=(0, 20, 120, 20, 0), ysplit=(0, 20, 16),
+        zsplit=(0, 20, 20), n1=200, sita_t=1e-5, sfa1=1.5, sfa2=2.0, T0=1e-3, Tn=0.3, Nt=41,
+        comps=(1, 1, 0, 0, 1, 1), model=dict(kind="uniform", sigma=1.0),
+        receivers=[(250.0 * (i + 1), 0.0, 0.0) for i in range(4)],
+        transmitters=[dict(ort=1, len=25.0, x=0.0, y=0.0, z=0.0)],
+    ),
     # survey config 2: 1-D marine model, 128 x 128 x 96 at 20 m
     "cfg2": _base(
         dmin=(20.0, 20.0, 20.0), arg1=1.06, arg2=1.15, xsplit=(6, 14, 48, 50, 10), ysplit=(6, 14, 88),
