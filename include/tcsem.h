@@ -51,7 +51,10 @@ typedef struct {
     int zchunks;          /* z-chunks of the fused sweep, 0 = chosen from the grid and the GPU */
     int serial_boundary;  /* 1: boundary pipeline strictly before the whole sweep; default 0 = the
                              boundary and the top z-chunk run beside the lower chunks */
-    int reserved[2];
+    int top_planes;       /* planes of the top z-chunk, 0 = default (one plane beside the boundary, so
+                             that little of the sweep waits for it; an even split with
+                             serial_boundary), -1 = an even split */
+    int reserved;
 } tcsem_opts;
 
 typedef struct {
@@ -62,6 +65,8 @@ typedef struct {
     int precision;
     size_t device_bytes;  /* device memory held by the handle */
     int launches_per_step; /* kernels launched per time step by tcsem_advance */
+    int zchunks;          /* z-chunks of the fused sweep in use */
+    int top_planes;       /* planes of the top z-chunk when it runs beside the others, else 0 */
 } tcsem_info;
 
 /* Opening a survey.  tcsem_open_dir reads FDTD_setup.in, Cond.bin, Receiver.in

@@ -28,14 +28,15 @@ class TcsemError(RuntimeError):
 
 class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("fix_dual_bipole", C.c_int), ("graph_steps", C.c_int),
-                ("zchunks", C.c_int), ("serial_boundary", C.c_int), ("reserved", C.c_int * 2)]
+                ("zchunks", C.c_int), ("serial_boundary", C.c_int), ("top_planes", C.c_int),
+                ("reserved", C.c_int)]
 
 
 class Info(C.Structure):
     _fields_ = [("L", C.c_int), ("M", C.c_int), ("N", C.c_int), ("L1", C.c_int), ("M1", C.c_int),
                 ("NRx", C.c_int), ("NTx", C.c_int), ("Nt", C.c_int), ("NComp", C.c_int), ("nefcmp", C.c_int),
                 ("nsteps", C.c_long), ("precision", C.c_int), ("device_bytes", C.c_size_t),
-                ("launches_per_step", C.c_int)]
+                ("launches_per_step", C.c_int), ("zchunks", C.c_int), ("top_planes", C.c_int)]
 
 
 def declared_functions():
@@ -114,13 +115,14 @@ class Simulation:
     """One survey on one GPU: the handle of include/tcsem.h."""
 
     def __init__(self, directory, precision=32, device=0, fix_dual_bipole=False, graph_steps=0, zchunks=0,
-                 serial_boundary=False):
+                 serial_boundary=False, top_planes=0):
         L = library()
         o = Opts()
         L.tcsem_default_opts(C.byref(o))
         o.precision, o.device, o.fix_dual_bipole, o.graph_steps = precision, device, int(fix_dual_bipole), graph_steps
         o.zchunks = zchunks
         o.serial_boundary = int(serial_boundary)
+        o.top_planes = top_planes
         h = C.c_void_p()
         st = L.tcsem_open_dir(os.fsencode(directory), C.byref(o), C.byref(h))
         if st != 0:
@@ -254,11 +256,12 @@ class Simulation:
 class Batch:
     """Many surveys advanced together (tcsem_batch_* of include/tcsem.h)."""
 
-    def __init__(self, precision=32, device=0, budget=0, graph_steps=0, zchunks=0):
+    def __init__(self, precision=32, device=0, budget=0, graph_steps=0, zchunks=0, top_planes=0):
         L = library()
         o = Opts()
         L.tcsem_default_opts(C.byref(o))
         o.precision, o.device, o.graph_steps, o.zchunks = precision, device, graph_steps, zchunks
+        o.top_planes = top_planes
         h = C.c_void_p()
         st = L.tcsem_batch_create(C.byref(o), int(budget), C.byref(h))
         if st != 0:

@@ -98,8 +98,9 @@ template <typename T> struct BatchImpl : BatchBase {
         if ((int)slots.size() >= kMaxSlots) throw Error(TCSEM_ERR_NOMEM, "the batch holds 64 slots");
         auto sim = std::make_unique<SimImpl<T>>();
         sim->opts = opts;
-        // the slots fill the GPU together: two z-chunks each (the top one overlaps the boundary) unless set
-        if (sim->opts.zchunks <= 0) sim->opts.zchunks = 2;
+        // the slots fill the GPU together: one z-chunk each unless set (no halo planes; the
+        // boundary kernels of all slots run as wide launches before the sweep)
+        if (sim->opts.zchunks <= 0) sim->opts.zchunks = 1;
         sim->device = device;
         sim->model.build(read_survey_dir(dir));
         sim->sched = sim->model.schedule();

@@ -76,11 +76,20 @@ struct StepGate {
     __device__ __forceinline__ long step() const { return (long)*base + off; }
 };
 
-// z-chunks of the fused sweep: chunk c covers planes [kb[c], kb[c+1])
+// z-chunks of the fused sweep: chunk c covers planes [kb[c], kb[c+1]); the
+// top chunk may be shorter than the others (it runs after the boundary)
 constexpr int kMaxChunks = 16;
 struct ZChunks {
     int n;
     int kb[kMaxChunks + 1];
+    // kb[c] for a run-time c without indexing the array (it may live in the
+    // kernel's parameter space)
+    __host__ __device__ __forceinline__ int plane(int c) const {
+        int v = 0;
+#pragma unroll
+        for (int q = 0; q <= kMaxChunks; q++) v = q == c ? kb[q] : v;
+        return v;
+    }
 };
 
 // ----------------------------------------------------------------- launchers
@@ -94,12 +103,17 @@ void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, cu
 struct SweepMaps {
     CUtensorMap m[7];
 };
+// chunks c0 .. c1-1 in one launch; rev = the last chunk's blocks first (consecutive
+// steps alternate, so a step starts on the planes the previous one wrote last,
+// which may still be in L2)
 template <typename T>
 void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
                         const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
-                        const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, int *err, cudaStream_t st);
+                        const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, bool rev, int *err,
+                        cudaStream_t st);
 template <typename T> cudaError_t sweep_configure(int N);
 template <typename T> size_t sweep_smem_bytes(int N);
+template <typename T> int sweep_blocks_per_sm(int N);  // resident sweep CTAs per SM (after sweep_configure)
 int sweep_box_x();
 int sweep_box_y();
 template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, const ZChunks &zc, cudaStream_t st);

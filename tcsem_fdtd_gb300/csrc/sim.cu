@@ -96,6 +96,8 @@ tcsem_status tcsem_get_info(const tcsem_sim_t *s, tcsem_info *o) {
     o->precision = b.opts.precision;
     o->device_bytes = b.dev_bytes;
     o->launches_per_step = b.launches_per_step;
+    o->zchunks = b.chunks_used;
+    o->top_planes = b.top_used;
     return TCSEM_OK;
 }
 

@@ -111,6 +111,7 @@ struct SimBase {
     long step = 0;
     size_t dev_bytes = 0;
     int launches_per_step = 0;
+    int chunks_used = 0, top_used = 0;  // z-chunk layout of the sweep in use (top_used 0: an even split)
     virtual ~SimBase() {}
     virtual void init() = 0;
     virtual void select(int itx) = 0;
@@ -259,19 +260,49 @@ template <typename T> struct SimImpl : SimBase {
         }
         launches_per_step = 4 + (overlap ? 2 : 1) + 1;
         CK(cudaStreamSynchronize(stream));
+        chunks_used = zc.n;
+        top_used = overlap ? zc.kb[1] : 0;
     }
 
-    // z-chunks of the fused sweep: enough CTAs to fill the GPU several times over
+    // z-chunk layout: n chunks, the top one `top` planes deep (top <= 0: an even split)
+    void set_chunks(int n, int top) {
+        const int N = model.N;
+        zc.n = n;
+        for (int c = 0; c <= n; c++) zc.kb[c] = (int)(((long)c * N) / n);
+        if (n > 1 && top > 0) {
+            top = std::max(1, std::min(top, N - (n - 1)));
+            for (int c = 1; c <= n; c++) zc.kb[c] = top + (int)(((long)(c - 1) * (N - top)) / (n - 1));
+        }
+    }
+    // most chunks a layout may have: every chunk keeps at least 8 planes
+    int max_chunks() const { return std::max(1, std::min(kMaxChunks, model.N / 8)); }
+    // z-chunks of the fused sweep.  Overlapped step: a one-plane top chunk (the only part of
+    // the sweep that waits for the boundary) and lower chunks whose CTAs fit in one wave;
+    // deeper chunks also mean fewer halo planes.  In FP32 the sweep is bound by memory and
+    // the wave leaves about 15 % of the CTA slots to the boundary kernels running beside it;
+    // in FP64 it is bound by the FP64 pipes and the wave fills the slots as far as it can.
+    // Serial step: enough CTAs to fill the GPU several times over, split evenly.
     void init_chunks() {
         const Model &m = model;
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        const long tiles = (long)((m.L + 63) / 64) * ((m.M + 7) / 8);  // 64 x 8 tiles of the fused sweep
-        int n = (int)std::min<long>(kMaxChunks, std::max<long>(1, (7L * sms + tiles - 1) / tiles));
-        n = std::min(n, std::max(1, m.N / 8));
+        CK(sweep_configure<T>(m.N));
+        const long tiles = (long)sweep_tiles_x(m.L) * sweep_tiles_y(m.M);
+        const long slots = (long)sms * sweep_blocks_per_sm<T>(m.N);
+        int n, top = 0;
+        if (opts.serial_boundary) {
+            n = (int)std::min<long>(kMaxChunks, std::max<long>(1, (7L * sms + tiles - 1) / tiles));
+        } else {
+            const long want = slots * 85 / 100;
+            long lower = std::max<long>(1, want / tiles);
+            if (sizeof(T) == 8 && (lower + 1) * tiles <= slots) lower++;
+            n = 1 + (int)lower;
+            top = 1;
+        }
+        n = std::min(n, max_chunks());
         if (opts.zchunks > 0) n = std::min(std::min(opts.zchunks, kMaxChunks), m.N);
-        zc.n = n;
-        for (int c = 0; c <= n; c++) zc.kb[c] = (int)(((long)c * m.N) / n);
+        if (opts.top_planes != 0) top = opts.top_planes;  // > 0: that many planes, < 0: an even split
+        set_chunks(n, top);
         const size_t tb = (size_t)n * g.PS * sizeof(T);
         for (int b = 0; b < 2; b++) {
             tot[b].alloc(tb);
@@ -314,7 +345,7 @@ template <typename T> struct SimImpl : SimBase {
     void sweep(int b, StepScalars<T> s, const StepScalars<T> *table, StepGate gate, int c0 = 0, int c1 = -1,
                cudaStream_t st = nullptr) {
         launch_fused_sweep<T>(maps[b], g, fs(b ^ 1), tot[b].as<T>(), tot[b ^ 1].as<T>(), ax, s, table, gate, src, zc,
-                              c0, c1 < 0 ? zc.n : c1, errw.as<int>(), st ? st : stream);
+                              c0, c1 < 0 ? zc.n : c1, (b & 1) != 0, errw.as<int>(), st ? st : stream);
     }
     void consolidate(int b) { launch_bz_consolidate<T>(g, fs(b).bz, tot[b].as<T>(), zc, stream); }
 

@@ -358,8 +358,8 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
     const int L = g.L, M = g.M, N = g.N, XP = g.XP;
     t.N = N;
     t.PS = (int)g.PS;
-    t.k0 = (c * N) / zc.n;  // = zc.kb[c]
-    t.k1 = ((c + 1) * N) / zc.n;
+    t.k0 = zc.plane(c);
+    t.k1 = zc.plane(c + 1);
     const int ty = w < 9 ? w : lane;
     t.j = t.j0 + ty;
     const bool rowok = w < 9 || lane <= BY;
@@ -490,14 +490,15 @@ template <typename T>
 __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1)
     k_sweep(const __grid_constant__ SweepMaps maps, Geom g, FieldSet<T> out, const T *__restrict__ tin,
             T *__restrict__ tout, Axis<T> ax, StepScalars<T> sdir, const StepScalars<T> *__restrict__ table,
-            StepGate gate, SourceTable<T> src, ZChunks zc, int cbase, int *err) {
+            StepGate gate, SourceTable<T> src, ZChunks zc, int cbase, int rev, int *err) {
     StepScalars<T> s = sdir;
     if (gate.base) {
         const long st = gate.step();
         if (st >= gate.nsteps) return;
         s = table[st];
     }
-    sweep_cta<T>(maps, g, out, tin, tout, ax, s, src, zc, blockIdx.x, blockIdx.y, cbase + blockIdx.z, err);
+    const int c = cbase + (int)(rev ? gridDim.z - 1 - blockIdx.z : blockIdx.z);
+    sweep_cta<T>(maps, g, out, tin, tout, ax, s, src, zc, blockIdx.x, blockIdx.y, c, err);
 }
 
 // every slot of a batch in one launch: block b belongs to the slot whose range of idx holds it
@@ -516,10 +517,11 @@ __global__ void __launch_bounds__(fs3::NT, sizeof(T) == 4 ? 2 : 1)
 template <typename T>
 void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
                         const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
-                        const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, int *err, cudaStream_t st) {
+                        const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, bool rev, int *err,
+                        cudaStream_t st) {
     dim3 grd((g.L + fs3::TX - 1) / fs3::TX, (g.M + fs3::BY - 1) / fs3::BY, c1 - c0);
     k_sweep<T><<<grd, fs3::NT, fs3::smem_bytes_n<T>(g.N), st>>>(maps, g, out, tin, tout, ax, s, table, gate, src, zc,
-                                                                c0, err);
+                                                                c0, rev ? 1 : 0, err);
 }
 
 template <typename T>
@@ -537,6 +539,12 @@ template <typename T> cudaError_t sweep_configure(int N) {
     return cudaFuncSetAttribute(k_sweep_batched<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
 }
 template <typename T> size_t sweep_smem_bytes(int N) { return fs3::smem_bytes_n<T>(N); }
+template <typename T> int sweep_blocks_per_sm(int N) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sweep<T>, fs3::NT, fs3::smem_bytes_n<T>(N)) != cudaSuccess)
+        return 1;
+    return nb > 0 ? nb : 1;
+}
 int sweep_box_x() { return fs3::BXW; }
 int sweep_box_y() { return fs3::BYH; }
 
@@ -567,9 +575,10 @@ template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, c
     template void launch_bderivate<T>(const Geom &, FieldSet<T>, const Axis<T> &, T, cudaStream_t);                \
     template void launch_fused_sweep<T>(const SweepMaps &, const Geom &, FieldSet<T>, const T *, T *,             \
                                         const Axis<T> &, StepScalars<T>, const StepScalars<T> *, StepGate,         \
-                                        const SourceTable<T> &, const ZChunks &, int, int, int *, cudaStream_t);             \
+                                        const SourceTable<T> &, const ZChunks &, int, int, bool, int *, cudaStream_t);       \
     template cudaError_t sweep_configure<T>(int);                                                                  \
     template size_t sweep_smem_bytes<T>(int);                                                                      \
+    template int sweep_blocks_per_sm<T>(int);                                                                      \
     template void launch_bz_consolidate<T>(const Geom &, T *, T *, const ZChunks &, cudaStream_t);             \
     template void launch_sweep_batched<T>(const SweepSlot<T> *, const BatchIndex &, int, int, int, cudaStream_t);
 INST(float)

@@ -1,8 +1,8 @@
 """Batched form: several surveys of different sizes advanced together.
 
 Each slot's traces must equal the same survey run alone through
-tcsem_run with the same z-chunk count (two, the batch default; the batched
-launches run the same per-CTA code on the same data): the check allows
+tcsem_run with the same z-chunk layout (one chunk, the batch default; the
+batched launches run the same per-CTA code on the same data): the check allows
 1e-12 (FP64) / 1e-6 (FP32) relative to each trace's peak.
 Slots join while others run and leave when done; admission respects the
 device-memory budget.
@@ -31,7 +31,7 @@ def built():
 def alone(d, precision, itx=0):
     from tcsem_fdtd_gb300 import Simulation
 
-    with Simulation(d, precision=precision, zchunks=2) as sim:
+    with Simulation(d, precision=precision, zchunks=1) as sim:
         return sim.run(itx)
 
 
@@ -120,4 +120,4 @@ def test_cli_batch_mode_writes_the_same_files(built, case_dir, tmp_path):
     for k in range(1, 7):
         (h1, a), (h2, b) = out["serial"][k], out["batch"][k]
         assert h1 == h2
-        assert rel_err(b, a) <= 1e-4  # FP32; two z-chunks per batch slot vs the single-survey default
+        assert rel_err(b, a) <= 1e-4  # FP32; one z-chunk per batch slot vs the single-survey layout

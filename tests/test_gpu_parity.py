@@ -231,16 +231,19 @@ def test_repeat_runs_are_bitwise_identical(built, case_dir):
 @pytest.mark.parametrize("precision", [64, 32])
 def test_overlapped_boundary_equals_serial_order(built, case_dir, precision):
     """Boundary + top z-chunk on a second stream beside the lower chunks gives the same bits as
-    running the boundary before the whole sweep (the two branches touch disjoint data)."""
+    running the boundary before the whole sweep (the two branches touch disjoint data), for
+    the same chunk layout: the default one-plane top chunk and an even split."""
     from tcsem_fdtd_gb300 import Simulation
 
     d = case_dir("small")
-    runs = []
-    for serial in (False, True):
-        with Simulation(d, precision=precision, zchunks=3, serial_boundary=serial) as sim:
-            assert sim.info["launches_per_step"] == (6 if serial else 7)
-            runs.append(sim.run(0))
-    np.testing.assert_array_equal(runs[0], runs[1])
+    for top in (1, -1):
+        runs = []
+        for serial in (False, True):
+            with Simulation(d, precision=precision, zchunks=3, top_planes=top, serial_boundary=serial) as sim:
+                assert sim.info["launches_per_step"] == (6 if serial else 7)
+                assert sim.info["zchunks"] == 3
+                runs.append(sim.run(0))
+        np.testing.assert_array_equal(runs[0], runs[1])
 
 
 def test_cli_writes_reference_formats(built, case_dir, tmp_path):

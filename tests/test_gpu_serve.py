@@ -1,7 +1,7 @@
 """Serving loop: requests arriving over time share the device batch.
 
 Every request's traces must be the same served in the mix as run alone
-(same z-chunk count): within 1e-6 relative to each trace's peak (FP32).  A
+(same z-chunk layout: one chunk): within 1e-6 relative to each trace's peak (FP32).  A
 budget that fits only part of the stream makes later requests wait for
 earlier ones to leave; they still complete with the same results.
 """
@@ -27,7 +27,7 @@ def built():
 def alone(d, itx=0):
     from tcsem_fdtd_gb300 import Simulation
 
-    with Simulation(d, precision=32, zchunks=2) as sim:
+    with Simulation(d, precision=32, zchunks=1) as sim:
         return sim.run(itx)
 
 
