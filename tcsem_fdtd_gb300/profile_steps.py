@@ -1,10 +1,13 @@
 """Run a few time steps of a named synthetic workload, for profilers.
 
     python -m tcsem_fdtd_gb300.profile_steps [--workload cfg3] [--steps 16]
-                                             [--precision 32] [--serial-boundary]
+                                             [--precision 32] [--serial-boundary] [--fused N]
 
 Writes the workload's input files to a temporary directory, opens it through
 the C ABI and advances `--steps` steps (CUDA graphs of 8 steps), then exits.
+With `--fused N` it instead launches the fused sweep alone N times
+(tcsem_fused_step: every z-chunk of the default layout in one launch, the
+launch bench.py times for the roofline).
 It reports nothing about speed: time with bench.py, and use this under ncu to
 get a launch list or a capture of one kernel on a short run.
 """
@@ -25,11 +28,19 @@ def main(argv=None):
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--serial-boundary", action="store_true",
                     help="boundary pipeline before one launch of the whole sweep (no overlap)")
+    ap.add_argument("--fused", type=int, default=0, help="launch the fused sweep alone this many times")
     a = ap.parse_args(argv)
     d = tempfile.mkdtemp(prefix=f"tcsem_prof_{a.workload}_")
     inputs.write_case(inputs.case(a.workload), d)
     with Simulation(d, precision=a.precision, graph_steps=8, serial_boundary=a.serial_boundary) as sim:
         sim.begin(0)
+        if a.fused:
+            sc = sim.schedule()
+            for q in range(a.fused):
+                sim.fused_step(sc["lam"][q], sc["dt1"][q], 0.5 * (sc["dt1"][q] + sc["dt2"][q]), 0.0)
+            sim.synchronize()
+            print(f"{a.workload}: {a.fused} fused sweeps, {sim.info['zchunks']} z-chunks", flush=True)
+            return 0
         sim.advance(a.steps)
         sim.synchronize()
         print(f"{a.workload}: {a.steps} steps, {sim.info['launches_per_step']} launches per step", flush=True)
