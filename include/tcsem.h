@@ -54,7 +54,11 @@ typedef struct {
     int top_planes;       /* planes of the top z-chunk, 0 = default (one plane beside the boundary, so
                              that little of the sweep waits for it; an even split with
                              serial_boundary), -1 = an even split */
-    int reserved;
+    int padded_plane;     /* continue the air field on a wider transform plane whose points beyond
+                             the uniform grid taper from its edge values to zero (raised cosine,
+                             the padding UpContinuation.cpp:21-49 sketches): 1 = the powers of two
+                             above L1 and M1, 2 = the smallest lengths >= L1, M1 without prime
+                             factors above 5; not the reference's arithmetic (default 0) */
 } tcsem_opts;
 
 typedef struct {

@@ -57,6 +57,7 @@ def lib():
         L.orc_bderivate.argtypes = [C.c_void_p, C.c_double]
         L.orc_spline_remap.argtypes = [C.c_void_p]
         L.orc_upcontinuation.argtypes = [C.c_void_p]
+        L.orc_upcontinuation_padded.argtypes = [C.c_void_p]
         L.orc_rx_interp.restype = C.c_double
         L.orc_rx_interp.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_run.restype = C.c_long
@@ -64,6 +65,7 @@ def lib():
         L.orc_schedule.restype = C.c_long
         L.orc_schedule.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long]
         L.orc_set_dual_bipole_compat.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_padded_plane.argtypes = [C.c_void_p, C.c_int]
         L.orc_num_threads.restype = C.c_int
     return _lib
 
@@ -167,11 +169,21 @@ class Oracle:
     def upcontinuation(self):
         lib().orc_upcontinuation(self.h)
 
+    def upcontinuation_padded(self):
+        """The padded-plane variant of the continuation (not the reference's arithmetic), in the
+        mode set by set_padded_plane (powers of two when unset)."""
+        lib().orc_upcontinuation_padded(self.h)
+
     def rx_interp(self, comp, ir):
         return lib().orc_rx_interp(self.h, comp, ir)
 
     def set_dual_bipole_compat(self, on):
         lib().orc_set_dual_bipole_compat(self.h, int(bool(on)))
+
+    def set_padded_plane(self, mode):
+        """Whole runs continue the air field on the padded plane (orc_upcontinuation_padded):
+        0 off, 1 powers of two, 2 lengths without prime factors above 5."""
+        lib().orc_set_padded_plane(self.h, int(mode))
 
     def run(self, itx=0, max_steps=-1):
         iv, _, _ = self.tx(itx)

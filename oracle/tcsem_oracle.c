@@ -79,6 +79,7 @@ typedef struct {
     double *ef0, *efs;
     int cur_tx;
     int bug_compat_dual_bipole; /* D3: second bipole injected at the first bipole's cells */
+    int padded_plane;           /* the time loop uses orc_upcontinuation_padded */
     char err[256];
 } orc_sim;
 
@@ -665,6 +666,8 @@ int orc_set_field(orc_sim *S, int comp, const double *in) {
     return 0;
 }
 void orc_set_dual_bipole_compat(orc_sim *S, int on) { S->bug_compat_dual_bipole = on; }
+void orc_upcontinuation_padded(orc_sim *S);
+void orc_set_padded_plane(orc_sim *S, int on) { S->padded_plane = on; }
 
 /* prepare_free_mem.cu:164-186 */
 void orc_zero_fields(orc_sim *S) {
@@ -1051,31 +1054,33 @@ static void c2r_2d(int M1, int L1, const cplx *F, double *a) {
     free(G);
 }
 
-/* FBz_to_FBxFBy, UpContinuation_gpu.cu:113-164 */
-static void continuation_multiply(orc_sim *S) {
-    const int L = S->L1, M = S->M1, H = L / 2 + 1;
+/* FBz_to_FBxFBy, UpContinuation_gpu.cu:113-164, on an L x M transform plane */
+static void continuation_multiply_on(const orc_sim *S, int L, int M, const cplx *FBz, cplx *FBx, cplx *FBy) {
+    const int H = L / 2 + 1;
     for (int iy = 0; iy < M; iy++) {
         double v1 = iy < M / 2 + 1 ? (1.0 * ORC_PI * iy) / M * (S->dzmin / S->dymin)
                                    : -(1.0 * ORC_PI * (M - iy)) / M * (S->dzmin / S->dymin);
         for (int ix = 0; ix < H; ix++) {
             double u1 = (1.0 * ORC_PI * ix) / L * (S->dzmin / S->dxmin);
-            cplx f = S->FBzC[(size_t)iy * H + ix];
+            cplx f = FBz[(size_t)iy * H + ix];
             cplx a = -cimag(f) + I * creal(f);
             if (ix == 0 && iy == 0) {
-                S->FBxC[0] = a; S->FByC[0] = a;
+                FBx[0] = a; FBy[0] = a;
             } else {
                 double upcc = exp(-sqrt(u1 * u1 + v1 * v1)) * (1.0 / sqrt(u1 * u1 + v1 * v1));
-                S->FBxC[(size_t)iy * H + ix] = (S->dxmin / S->dymin) * u1 * upcc * a;
-                S->FByC[(size_t)iy * H + ix] = (S->dymin / S->dxmin) * v1 * upcc * a;
+                FBx[(size_t)iy * H + ix] = (S->dxmin / S->dymin) * u1 * upcc * a;
+                FBy[(size_t)iy * H + ix] = (S->dymin / S->dxmin) * v1 * upcc * a;
             }
         }
     }
 }
+static void continuation_multiply(orc_sim *S) {
+    continuation_multiply_on(S, S->L1, S->M1, S->FBzC, S->FBxC, S->FByC);
+}
 
 /* Blinear_BxR2IR / Blinear_ByR2IR, UpContinuation_gpu.cu:42-110 */
-static void bilinear_back(orc_sim *S) {
+static void bilinear_back_norm(orc_sim *S, double norm) {
     const int L0 = S->L, M0 = S->M, L1 = S->L1, M1 = S->M1;
-    const double norm = (double)(L1 * M1);
     for (int iy = 0; iy < M0; iy++)
         for (int ix = 0; ix < L0 + 1; ix++) {
             int II = S->xoldBx2NewBz[ix]; II = II < 1 ? 1 : II; II = II > L1 - 1 ? L1 - 1 : II;
@@ -1100,6 +1105,8 @@ static void bilinear_back(orc_sim *S) {
         }
 }
 
+static void bilinear_back(orc_sim *S) { bilinear_back_norm(S, (double)(S->L1 * S->M1)); }
+
 /* UpContinuation_gpu, UpContinuation_gpu.cu:166-274 */
 void orc_upcontinuation(orc_sim *S) {
     orc_spline_remap(S);
@@ -1108,6 +1115,69 @@ void orc_upcontinuation(orc_sim *S) {
     c2r_2d(S->M1, S->L1, S->FBxC, S->FBxR);
     c2r_2d(S->M1, S->L1, S->FByC, S->FByR);
     bilinear_back(S);
+}
+
+/* The padded variant (not the reference's arithmetic; the padding that
+ * UpContinuation.cpp:21-49 sketches, with the plane sizes of
+ * ModelingSetup.cpp:194-195 in mode 1): the uniform plane is centred in a
+ * plane of the next powers of two above L1 and M1 (mode 1) or of the smallest
+ * lengths >= L1, M1 without prime factors above 5 (mode 2; padded_plane as set
+ * by orc_set_padded_plane, mode 1 when unset), each row is continued left of the grid
+ * by its first value and right of it by its last value times a raised-cosine
+ * taper to zero, then each column of the widened plane likewise; the
+ * continuation runs on that plane and the grid part goes to the bilinear
+ * remap, normalised by the padded size. */
+static int orc_plane_len(int n, int mode) {
+    if (mode == 1) { int p = 1; while (p <= n) p *= 2; return p; }
+    if (mode == 2)
+        for (int m = n;; m++) {
+            int r = m;
+            while (r % 2 == 0) r /= 2;
+            while (r % 3 == 0) r /= 3;
+            while (r % 5 == 0) r /= 5;
+            if (r == 1) return m;
+        }
+    return n;
+}
+static double orc_taper(int i, int n, int nu, int d) {
+    if (i < d) return 0.5 * (1.0 - cos(ORC_PI * i / d));
+    return 0.5 * (1.0 - cos(ORC_PI * (n - i) / (n - nu - d + 1)));
+}
+void orc_upcontinuation_padded(orc_sim *S) {
+    orc_spline_remap(S);
+    const int mode = S->padded_plane > 0 ? S->padded_plane : 1;
+    const int L1 = S->L1, M1 = S->M1, Lf = orc_plane_len(L1, mode), Mf = orc_plane_len(M1, mode);
+    const int DL = (Lf - L1) / 2, DM = (Mf - M1) / 2, H = Lf / 2 + 1;
+    double *P = (double *)calloc((size_t)Lf * Mf, sizeof(double));
+    for (int y = 0; y < M1; y++) {
+        double *row = P + (size_t)(DM + y) * Lf;
+        const double *src = S->BzAir + (size_t)y * L1;
+        for (int x = 0; x < L1; x++) row[DL + x] = src[x];
+        for (int x = 0; x < Lf; x++)
+            if (x < DL || x >= DL + L1) row[x] = orc_taper(x, Lf, L1, DL) * (x < DL ? src[0] : src[L1 - 1]);
+    }
+    for (int y = 0; y < Mf; y++) {
+        if (y >= DM && y < DM + M1) continue;
+        const double w = orc_taper(y, Mf, M1, DM);
+        const double *edge = P + (size_t)(y < DM ? DM : DM + M1 - 1) * Lf;
+        for (int x = 0; x < Lf; x++) P[(size_t)y * Lf + x] = w * edge[x];
+    }
+    cplx *Fz = (cplx *)malloc((size_t)Mf * H * sizeof(cplx));
+    cplx *Fx = (cplx *)malloc((size_t)Mf * H * sizeof(cplx));
+    cplx *Fy = (cplx *)malloc((size_t)Mf * H * sizeof(cplx));
+    double *Rx = (double *)malloc((size_t)Lf * Mf * sizeof(double));
+    double *Ry = (double *)malloc((size_t)Lf * Mf * sizeof(double));
+    r2c_2d(Mf, Lf, P, Fz);
+    continuation_multiply_on(S, Lf, Mf, Fz, Fx, Fy);
+    c2r_2d(Mf, Lf, Fx, Rx);
+    c2r_2d(Mf, Lf, Fy, Ry);
+    for (int y = 0; y < M1; y++)
+        for (int x = 0; x < L1; x++) {
+            S->FBxR[(size_t)y * L1 + x] = Rx[(size_t)(DM + y) * Lf + DL + x];
+            S->FByR[(size_t)y * L1 + x] = Ry[(size_t)(DM + y) * Lf + DL + x];
+        }
+    bilinear_back_norm(S, (double)Lf * (double)Mf);
+    free(P); free(Fz); free(Fx); free(Fy); free(Rx); free(Ry);
 }
 
 /* ---------------------------------------------------- receiver sampling */
@@ -1269,7 +1339,8 @@ long orc_run(orc_sim *S, int itx, double *traces, long max_steps) {
     while (ne < S->Nt || (nb < S->Nt && S->nefcmp < S->NComp)) {
         if (max_steps >= 0 && steps >= max_steps) break;
         double nmuda = 7.5 * S->sfa2 * dt2 * dt1 / mu / mindx / mindx;
-        orc_upcontinuation(S);
+        if (S->padded_plane > 0) orc_upcontinuation_padded(S);
+        else orc_upcontinuation(S);
         orc_electric_field(S, itx, nmuda, dt1, n < 2 * S->nsrc ? S->wave[n] : 0);
         orc_bderivate(S, 0.5 * (dt1 + dt2));
         toT += dt1;

@@ -29,7 +29,7 @@ class TcsemError(RuntimeError):
 class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("fix_dual_bipole", C.c_int), ("graph_steps", C.c_int),
                 ("zchunks", C.c_int), ("serial_boundary", C.c_int), ("top_planes", C.c_int),
-                ("reserved", C.c_int)]
+                ("padded_plane", C.c_int)]
 
 
 class Info(C.Structure):
@@ -115,7 +115,7 @@ class Simulation:
     """One survey on one GPU: the handle of include/tcsem.h."""
 
     def __init__(self, directory, precision=32, device=0, fix_dual_bipole=False, graph_steps=0, zchunks=0,
-                 serial_boundary=False, top_planes=0):
+                 serial_boundary=False, top_planes=0, padded_plane=False):
         L = library()
         o = Opts()
         L.tcsem_default_opts(C.byref(o))
@@ -123,6 +123,7 @@ class Simulation:
         o.zchunks = zchunks
         o.serial_boundary = int(serial_boundary)
         o.top_planes = top_planes
+        o.padded_plane = int(padded_plane)  # 0, 1 (powers of two) or 2 (5-smooth lengths)
         h = C.c_void_p()
         st = L.tcsem_open_dir(os.fsencode(directory), C.byref(o), C.byref(h))
         if st != 0:
@@ -256,12 +257,13 @@ class Simulation:
 class Batch:
     """Many surveys advanced together (tcsem_batch_* of include/tcsem.h)."""
 
-    def __init__(self, precision=32, device=0, budget=0, graph_steps=0, zchunks=0, top_planes=0):
+    def __init__(self, precision=32, device=0, budget=0, graph_steps=0, zchunks=0, top_planes=0, padded_plane=False):
         L = library()
         o = Opts()
         L.tcsem_default_opts(C.byref(o))
         o.precision, o.device, o.graph_steps, o.zchunks = precision, device, graph_steps, zchunks
         o.top_planes = top_planes
+        o.padded_plane = int(padded_plane)
         h = C.c_void_p()
         st = L.tcsem_batch_create(C.byref(o), int(budget), C.byref(h))
         if st != 0:

@@ -104,7 +104,7 @@ template <typename T> struct BatchImpl : BatchBase {
         sim->device = device;
         sim->model.build(read_survey_dir(dir));
         sim->sched = sim->model.schedule();
-        const size_t est = SimImpl<T>::estimate_bytes(sim->model, sim->sched.nsteps);
+        const size_t est = SimImpl<T>::estimate_bytes(sim->model, sim->sched.nsteps, sim->opts.padded_plane);
         if (budget && used + est > budget)
             throw Error(TCSEM_ERR_NOMEM, "device budget: the survey needs about " + std::to_string(est) +
                                              " bytes, " + std::to_string(budget - std::min(budget, used)) + " are free");

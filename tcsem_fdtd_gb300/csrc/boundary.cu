@@ -123,6 +123,19 @@ __device__ __forceinline__ bool staged(uint64_t *bar, int *err) {
     return true;
 }
 
+// Padded plane: the n - nu points outside the grid [d, d + nu) of a line of n points are the
+// first grid value times w[i] left of the grid (i < d) and the last one times w[i] right of it.
+template <typename T>
+__device__ __forceinline__ void pad_line(C2<T> *a, int n, int nu, int d, const T *__restrict__ w) {
+    const C2<T> lo = a[d], hi = a[d + nu - 1];
+    for (int i = threadIdx.x; i < n - nu; i += blockDim.x) {
+        const int p = i < d ? i : i + nu;  // the pad points in order, skipping the grid
+        const T f = w[p];
+        const C2<T> e = p < d ? lo : hi;
+        a[p] = {f * e.x, f * e.y};
+    }
+}
+
 // ---- stage 1: x-remap of the M old rows + forward FFT along x.  Rows j0 and
 // j0+1 travel as the real and imaginary parts of one complex transform and are
 // separated in the spectrum: X1 = (Z[k] + conj Z[-k]) / 2, X2 = (Z[k] - conj Z[-k]) / 2i.
@@ -177,7 +190,7 @@ __device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *
         const StripPlan S = threadIdx.x < 2 ? R.s[0] : R.s[1];
         spline_solve(tab + S.f, S.n, row + (threadIdx.x & 1) * L + S.src, 1, mbuf + threadIdx.x * R.nmax);
     }
-    const int anl = bd.AnLx, AL = bd.AL;
+    const int anl = bd.AnLx + bd.DL, AL = bd.AL;
     for (int c = threadIdx.x; c < bd.Nx; c += blockDim.x) a[anl + c] = {r0[AL + c], r1[AL + c]};
     __syncthreads();
     const int np0 = R.s[0].npts, np = np0 + R.s[1].npts;
@@ -186,10 +199,14 @@ __device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *
         const StripPlan S = s ? R.s[1] : R.s[0];
         const int k0 = tabi[S.k + q];
         const T *c = tab + S.c + q, *m0 = mbuf + 2 * s * R.nmax + k0;
-        a[S.dst + q] = {spline_out(c, S.npts, r0 + S.src + k0, 1, m0),
-                        spline_out(c, S.npts, r1 + S.src + k0, 1, m0 + R.nmax)};
+        a[bd.DL + S.dst + q] = {spline_out(c, S.npts, r0 + S.src + k0, 1, m0),
+                                spline_out(c, S.npts, r1 + S.src + k0, 1, m0 + R.nmax)};
     }
     __syncthreads();
+    if (L1 != bd.Lu) {  // padded plane: taper the row from its edge values to zero
+        pad_line(a, L1, bd.Lu, bd.DL, bd.padx);
+        __syncthreads();
+    }
     const C2<T> *Z = fft::run<false, 1>(a, b, bd.px, tw);
     for (int kx = threadIdx.x; kx < bd.H; kx += blockDim.x) {
         const C2<T> zk = Z[kx], zm = Z[kx == 0 ? 0 : L1 - kx];
@@ -240,7 +257,7 @@ __device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
         spline_solve(tab + S.f, S.n, reinterpret_cast<const T *>(col + S.src) + (threadIdx.x & 1), 2,
                      mbuf + threadIdx.x * R.nmax);
     }
-    const int any = bd.Any, Ay = bd.Ay;
+    const int any = bd.Any + bd.DM, Ay = bd.Ay;
     for (int r = threadIdx.x; r < bd.Ny; r += blockDim.x) a[any + r] = col[Ay + r];
     __syncthreads();
     const int np0 = R.s[0].npts, np = np0 + R.s[1].npts;
@@ -250,9 +267,13 @@ __device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
         const int k0 = tabi[S.k + q];
         const T *c = tab + S.c + q, *m0 = mbuf + 2 * s * R.nmax + k0;
         const T *yb = reinterpret_cast<const T *>(col + S.src + k0);
-        a[S.dst + q] = {spline_out(c, S.npts, yb, 2, m0), spline_out(c, S.npts, yb + 1, 2, m0 + R.nmax)};
+        a[bd.DM + S.dst + q] = {spline_out(c, S.npts, yb, 2, m0), spline_out(c, S.npts, yb + 1, 2, m0 + R.nmax)};
     }
     __syncthreads();
+    if (M1 != bd.Mu) {  // padded plane: taper the column (x-frequency domain; the taper is linear)
+        pad_line(a, M1, bd.Mu, bd.DM, bd.pady);
+        __syncthreads();
+    }
     C2<T> *F = fft::run<false, 1>(a, b, bd.py, tw);
     // FBx = i*gx*F, FBy = i*gy*F (FBz_to_FBxFBy, UpContinuation_gpu.cu:113-164) side by side
     C2<T> *in = F == a ? b : a;
@@ -305,8 +326,8 @@ __device__ __forceinline__ void rows_inv_cta(const BoundaryDev<T> &bd, int blk) 
     }
     __syncthreads();
     const C2<T> *res = fft::run<true, 1>(a, b, bd.px, tw);
-    C2<T> *dst = bd.Z + (size_t)s * L1;
-    for (int x = threadIdx.x; x < L1; x += blockDim.x) dst[x] = res[x];
+    C2<T> *dst = bd.Z + (size_t)s * bd.Lu;
+    for (int x = threadIdx.x; x < bd.Lu; x += blockDim.x) dst[x] = res[bd.DL + x];
 }
 
 // ---- stage 4: bilinear remap (Blinear_BxR2IR / Blinear_ByR2IR, UpContinuation_gpu.cu:42-110)
@@ -320,7 +341,7 @@ __device__ __forceinline__ void bilinear_cta(const BoundaryDev<T> &bd, T *bx, T 
             const int j = e / (L + 1), i = e % (L + 1);
             const int II = bd.bxc_II[i];
             const T lx = bd.bxc_l[i];
-            const C2<T> *ra = bd.Z + (size_t)bd.bxr_a[j] * bd.L1, *rb = bd.Z + (size_t)bd.bxr_b[j] * bd.L1;
+            const C2<T> *ra = bd.Z + (size_t)bd.bxr_a[j] * bd.Lu, *rb = bd.Z + (size_t)bd.bxr_b[j] * bd.Lu;
             T a0 = (T(1) - lx) * ra[II - 1].x + lx * ra[II].x;
             T a1 = (T(1) - lx) * rb[II - 1].x + lx * rb[II].x;
             T ly = bd.bxr_l[j];
@@ -329,7 +350,7 @@ __device__ __forceinline__ void bilinear_cta(const BoundaryDev<T> &bd, T *bx, T 
             const int e2 = e - nbx, j = e2 / L, i = e2 % L;
             const int II = bd.byc_II[i];
             const T lx = bd.byc_l[i];
-            const C2<T> *ra = bd.Z + (size_t)bd.byr_a[j] * bd.L1, *rb = bd.Z + (size_t)bd.byr_b[j] * bd.L1;
+            const C2<T> *ra = bd.Z + (size_t)bd.byr_a[j] * bd.Lu, *rb = bd.Z + (size_t)bd.byr_b[j] * bd.Lu;
             T a0 = (T(1) - lx) * ra[II - 1].y + lx * ra[II].y;
             T a1 = (T(1) - lx) * rb[II - 1].y + lx * rb[II].y;
             T ly = bd.byr_l[j];

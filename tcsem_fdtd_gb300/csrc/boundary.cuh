@@ -33,8 +33,13 @@ template <typename T> struct AxisRemap {
 };
 
 template <typename T> struct BoundaryDev {
-    // plane geometry
+    // plane geometry: the transforms have L1 x M1 points; the uniform grid (Lu x Mu points)
+    // sits at offset (DL, DM) in them.  Without padding Lu = L1, Mu = M1, DL = DM = 0; with
+    // padding the points outside the grid taper each row (column) from its edge values to
+    // zero with the weights padx[L1] (pady[M1]), zero inside the grid.
     int L1, M1, H, M;          // H = L1/2 + 1 kept x-frequencies
+    int Lu, Mu, DL, DM;
+    const T *padx, *pady;
     int AnLx, Nx, AL;
     int Any, Ny, Ay;
     int Mp, M1p, Hp;           // padded strides of FT, Gx/Gy and VX/VY (16-byte rows)
@@ -48,7 +53,7 @@ template <typename T> struct BoundaryDev {
     int S;
     const int *rows;
     // scratch
-    C2<T> *FT, *VX, *VY, *Z;  // FT is [H][Mp]; VX, VY are [S][Hp]; Z is [S][L1]
+    C2<T> *FT, *VX, *VY, *Z;  // FT is [H][Mp]; VX, VY are [S][Hp]; Z is [S][Lu]
     int *err;                 // device error word (a bounded wait gave up)
     // bilinear tables (indices already clamped as in the reference)
     const int *bxc_II, *bxr_a, *bxr_b, *byc_II, *byr_a, *byr_b;

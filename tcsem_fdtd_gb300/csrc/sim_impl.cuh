@@ -173,7 +173,7 @@ template <typename T> struct SimImpl : SimBase {
     DevMem axis_mem;
     Axis<T> ax{};
     // boundary
-    DevMem twx, twy, remT[2], remI[2], Gx, Gy, rows, FT, VX, VY, Zs;
+    DevMem twx, twy, remT[2], remI[2], Gx, Gy, rows, FT, VX, VY, Zs, padx, pady;
     DevMem bxc_II, bxr_a, bxr_b, byc_II, byr_a, byr_b, bxc_l, bxr_l, byc_l, byr_l;
     BoundaryDev<T> bd{};
     // step tables
@@ -349,9 +349,40 @@ template <typename T> struct SimImpl : SimBase {
     }
     void consolidate(int b) { launch_bz_consolidate<T>(g, fs(b).bz, tot[b].as<T>(), zc, stream); }
 
+    // transform length of a uniform line of n points: n itself (mode 0), the power of two
+    // above it (mode 1, the LNx2/LMy2 sizes of ModelingSetup.cpp:194-195), or the smallest
+    // length >= n with no prime factor above 5 (mode 2: only the FFT-friendly size)
+    static int plane_len(int n, int mode) {
+        if (mode == 1) {
+            int p = 1;
+            while (p <= n) p *= 2;
+            return p;
+        }
+        if (mode == 2)
+            for (int m = n;; m++) {
+                int r = m;
+                for (int f : {2, 3, 5})
+                    while (r % f == 0) r /= f;
+                if (r == 1) return m;
+            }
+        return n;
+    }
+    // raised-cosine weights of the padded points of a line of n transform points around a grid
+    // of nu points at offset d (the taper UpContinuation.cpp:21-49 sketches), zero on the grid
+    static std::vector<double> pad_weights(int n, int nu, int d) {
+        std::vector<double> w(n + 4, 0.0);  // 4 spare entries keep the upload a multiple of 16 bytes
+        const int r = n - nu - d;
+        for (int i = 0; i < d; i++) w[i] = 0.5 * (1.0 - std::cos(kPi * i / d));
+        for (int i = d + nu; i < n; i++) w[i] = 0.5 * (1.0 - std::cos(kPi * (n - i) / (r + 1)));
+        return w;
+    }
     void init_boundary() {
         const Model &m = model;
-        const int L1 = m.L1, M1 = m.M1, H = L1 / 2 + 1;
+        const int mode = opts.padded_plane;
+        if (mode < 0 || mode > 2) throw Error(TCSEM_ERR_INVALID, "padded_plane must be 0, 1 or 2");
+        const int Lu = m.L1, Mu = m.M1;                                 // the uniform grid
+        const int L1 = plane_len(Lu, mode), M1 = plane_len(Mu, mode);  // the transforms
+        const int H = L1 / 2 + 1, DL = (L1 - Lu) / 2, DM = (M1 - Mu) / 2;
         auto tw = [&](int n, DevMem &d) {
             std::vector<C2<T>> h(n + 1, C2<T>{T(0), T(0)});  // one spare entry: 16-byte bulk copies
             for (int k = 0; k < n; k++) {
@@ -426,33 +457,35 @@ template <typename T> struct SimImpl : SimBase {
         // rows of the uniform plane that the bilinear remap reads, and its tables
         auto clampi = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi); };
         std::vector<int> need;
-        for (int j = 0; j < m.M; j++) { int J = clampi(m.yBzold2New[j], 1, M1 - 1); need.push_back(J - 1); need.push_back(J); }
-        for (int j = 0; j <= m.M; j++) { int J = clampi(m.yoldBy2NewBz[j], 1, M1 - 1); need.push_back(J - 1); need.push_back(J); }
+        for (int j = 0; j < m.M; j++) { int J = clampi(m.yBzold2New[j], 1, Mu - 1); need.push_back(J - 1); need.push_back(J); }
+        for (int j = 0; j <= m.M; j++) { int J = clampi(m.yoldBy2NewBz[j], 1, Mu - 1); need.push_back(J - 1); need.push_back(J); }
         std::sort(need.begin(), need.end());
         need.erase(std::unique(need.begin(), need.end()), need.end());
-        std::vector<int> slot(M1, -1);
+        std::vector<int> slot(Mu, -1);
         for (size_t s = 0; s < need.size(); s++) slot[need[s]] = (int)s;
-        upload(rows, need);
+        std::vector<int> rows_t(need);  // rows of the transform plane
+        for (int &r : rows_t) r += DM;
+        upload(rows, rows_t);
         std::vector<int> hbxcII(m.L + 1), hbxra(m.M), hbxrb(m.M), hbycII(m.L), hbyra(m.M + 1), hbyrb(m.M + 1);
         std::vector<double> hbxcl(m.L + 1), hbxrl(m.M), hbycl(m.L), hbyrl(m.M + 1);
         for (int i = 0; i <= m.L; i++) {
-            int II = clampi(m.xoldBx2NewBz[i], 1, L1 - 1);
+            int II = clampi(m.xoldBx2NewBz[i], 1, Lu - 1);
             double Xp = i == m.L ? m.X[m.L - 1] + 0.5 * m.dx[m.L - 1] : m.X[i] - 0.5 * m.dx[i];
             hbxcII[i] = II;
             hbxcl[i] = (Xp - m.Xn[II - 1]) / (m.Xn[II] - m.Xn[II - 1]);
         }
         for (int j = 0; j < m.M; j++) {
-            int J = clampi(m.yBzold2New[j], 1, M1 - 1);
+            int J = clampi(m.yBzold2New[j], 1, Mu - 1);
             hbxra[j] = slot[J - 1]; hbxrb[j] = slot[J];
             hbxrl[j] = (m.Y[j] - m.Yn[J - 1]) / (m.Yn[J] - m.Yn[J - 1]);
         }
         for (int i = 0; i < m.L; i++) {
-            int II = clampi(m.xBzold2New[i], 1, L1 - 1);
+            int II = clampi(m.xBzold2New[i], 1, Lu - 1);
             hbycII[i] = II;
             hbycl[i] = (m.X[i] - m.Xn[II - 1]) / (m.Xn[II] - m.Xn[II - 1]);
         }
         for (int j = 0; j <= m.M; j++) {
-            int J = clampi(m.yoldBy2NewBz[j], 1, M1 - 1);
+            int J = clampi(m.yoldBy2NewBz[j], 1, Mu - 1);
             double Yp = j == m.M ? m.Y[m.M - 1] + 0.5 * m.dy[m.M - 1] : m.Y[j] - 0.5 * m.dy[j];
             hbyra[j] = slot[J - 1]; hbyrb[j] = slot[J];
             hbyrl[j] = (Yp - m.Yn[J - 1]) / (m.Yn[J] - m.Yn[J - 1]);
@@ -467,9 +500,13 @@ template <typename T> struct SimImpl : SimBase {
         FT.alloc((size_t)H * Mp * sizeof(C2<T>)); dev_bytes += FT.n;
         VX.alloc((size_t)S * Hp * sizeof(C2<T>)); dev_bytes += VX.n;
         VY.alloc((size_t)S * Hp * sizeof(C2<T>)); dev_bytes += VY.n;
-        Zs.alloc((size_t)S * L1 * sizeof(C2<T>)); dev_bytes += Zs.n;
+        Zs.alloc((size_t)S * Lu * sizeof(C2<T>)); dev_bytes += Zs.n;
+        upload(padx, conv(pad_weights(L1, Lu, DL)));
+        upload(pady, conv(pad_weights(M1, Mu, DM)));
         BoundaryDev<T> &B = bd;
         B.L1 = L1; B.M1 = M1; B.H = H; B.M = m.M;
+        B.Lu = Lu; B.Mu = Mu; B.DL = DL; B.DM = DM;
+        B.padx = padx.as<T>(); B.pady = pady.as<T>();
         B.AnLx = m.AnLx_New; B.Nx = m.in.Nx; B.AL = m.in.ALx1 + m.in.ALx2;
         B.Any = m.Any_New; B.Ny = m.in.Ny; B.Ay = m.in.Ay1 + m.in.Ay2;
         pack(0, m.sl, m.sr, m.ox, m.AnLx_New + m.in.Nx, B.rx);
@@ -653,9 +690,11 @@ template <typename T> struct SimImpl : SimBase {
     int sweep_blocks() const { return sweep_tiles_x(g.L) * sweep_tiles_y(g.M) * zc.n; }
     int rx_stencils() const { return rd.NComp * rd.nr; }
     // an upper bound of the device memory init() allocates, from the host model alone
-    static size_t estimate_bytes(const Model &m, long nsteps) {
+    static size_t estimate_bytes(const Model &m, long nsteps, int padded_plane) {
         const Geom gg = make_geom(m.L, m.M, m.N);
-        const size_t vol = (size_t)gg.total() * sizeof(T), H = m.L1 / 2 + 2, L1 = m.L1, M1 = m.M1;
+        const size_t vol = (size_t)gg.total() * sizeof(T), L1 = plane_len(m.L1, padded_plane),
+                     M1 = plane_len(m.M1, padded_plane);
+        const size_t H = L1 / 2 + 2;
         size_t b = 13 * vol + 2 * (size_t)kMaxChunks * gg.PS * sizeof(T);
         b += (H * (m.M + 2) + 2 * M1 * H + M1 * L1) * 2 * sizeof(T) + 2 * H * (M1 + 4) * sizeof(T);
         b += (size_t)nsteps * (sizeof(StepScalars<T>) + sizeof(StepEntryActs)) + ((size_t)4 << 20);

@@ -168,6 +168,32 @@ def test_full_run_fp32_within_one_percent(built, case_dir, name):
     assert err < 1e-2
 
 
+# transforms of mode 1 (powers of two): 128 x 128, 512 x 512, 1024 x 256; of mode 2 (no prime
+# factor above 5): 96 x 80, 450 x 270, 864 x 180
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("name", ["small", "cfg1", "cfg2"])
+def test_padded_upcontinuation_stage(built, case_dir, name, precision, mode):
+    """The padded-plane options against the oracle's padded continuation."""
+    sim, orc = pair(case_dir, name, precision, padded_plane=mode)
+    orc.set_padded_plane(mode)
+    randomize(sim, orc, 13, names=("Bz",))
+    sim.upcontinuation()
+    orc.upcontinuation_padded()
+    for n in ("BxAir", "ByAir"):
+        assert rel(sim.get(n), orc.get(n)) < BOUNDARY_TOL[precision], n
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_padded_plane_full_run(built, case_dir, precision, mode):
+    sim, orc = pair(case_dir, "small", precision, padded_plane=mode)
+    orc.set_padded_plane(mode)
+    exp, _ = orc.run(0)
+    got = sim.run(0, nr=exp.shape[0])
+    assert trace_error(got, exp) < (1e-8 if precision == 64 else 1e-2)
+
+
 def test_all_transmitter_orientations_fp64(built, case_dir):
     sim, orc = pair(case_dir, "txvar", 64)
     for t in range(orc.NTx):
