@@ -27,6 +27,15 @@ namespace tcsem {
 
 constexpr int kBndThreads = 256;
 
+// Programmatic dependent launch.  Each kernel of the chain lets the next one start once
+// its own transforms are done (the next one's blocks stage their tables while this one
+// writes its results); the next one waits for this grid's completion and memory before
+// it reads what this grid wrote.  Without the launch attribute the wait returns at once.
+// Releasing the next kernel only at the end keeps its waiting blocks from holding SM
+// resources that the sweep running beside the boundary needs.
+__device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait_prev() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Natural-spline second derivatives mb[0..n) of the line y[0..n) (stride ys)
 // from the precomputed elimination factors tab = g | w | inv | du; one thread
 // per line (n is at most 128).
@@ -208,6 +217,7 @@ __device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *
         __syncthreads();
     }
     const C2<T> *Z = fft::run<false, 1>(a, b, bd.px, tw);
+    pdl_allow_next();
     for (int kx = threadIdx.x; kx < bd.H; kx += blockDim.x) {
         const C2<T> zk = Z[kx], zm = Z[kx == 0 ? 0 : L1 - kx];
         C2<T> *dst = bd.FT + (size_t)kx * bd.Mp + j0;
@@ -244,9 +254,10 @@ __device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
         bulk_load(tw, bd.twy, btw, bar);
         bulk_load(tab, R.tabT, bt, bar);
         bulk_load(tabi, R.tabI, bi, bar);
-        bulk_load(col, bd.FT + (size_t)kx * bd.Mp, bc, bar);
         bulk_load(gx, bd.Gx + (size_t)kx * bd.M1p, bg, bar);
         bulk_load(gy, bd.Gy + (size_t)kx * bd.M1p, bg, bar);
+        pdl_wait_prev();  // FT is the previous kernel's output
+        bulk_load(col, bd.FT + (size_t)kx * bd.Mp, bc, bar);
     }
     __syncthreads();
     if (!staged(bar, bd.err)) return;
@@ -285,6 +296,7 @@ __device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
     }
     __syncthreads();
     const C2<T> *out = fft::run<true, 2>(in, F, bd.py, tw);
+    pdl_allow_next();
     for (int s = threadIdx.x; s < bd.S; s += blockDim.x) {
         const int rr = bd.rows[s];
         bd.VX[(size_t)s * bd.Hp + kx] = out[rr];
@@ -310,6 +322,7 @@ __device__ __forceinline__ void rows_inv_cta(const BoundaryDev<T> &bd, int blk) 
         mbar_init_fence();
         mbar_expect_tx(bar, btw + 2 * bv);
         bulk_load(tw, bd.twx, btw, bar);
+        pdl_wait_prev();  // VX and VY are the previous kernel's output
         bulk_load(vx, bd.VX + (size_t)s * bd.Hp, bv, bar);
         bulk_load(vy, bd.VY + (size_t)s * bd.Hp, bv, bar);
     }
@@ -326,6 +339,7 @@ __device__ __forceinline__ void rows_inv_cta(const BoundaryDev<T> &bd, int blk) 
     }
     __syncthreads();
     const C2<T> *res = fft::run<true, 1>(a, b, bd.px, tw);
+    pdl_allow_next();
     C2<T> *dst = bd.Z + (size_t)s * bd.Lu;
     for (int x = threadIdx.x; x < bd.Lu; x += blockDim.x) dst[x] = res[bd.DL + x];
 }
@@ -336,6 +350,7 @@ __device__ __forceinline__ void bilinear_cta(const BoundaryDev<T> &bd, T *bx, T 
     const int L = g.L, M = g.M;
     const int nbx = (L + 1) * M, nby = L * (M + 1);
     const T norm = bd.inv_norm;
+    pdl_wait_prev();  // Z is the previous kernel's output
     for (int e = blk * blockDim.x + threadIdx.x; e < nbx + nby; e += nblk * blockDim.x) {
         if (e < nbx) {
             const int j = e / (L + 1), i = e % (L + 1);
@@ -459,31 +474,48 @@ template <typename T> cudaError_t boundary_configure_batched(const size_t *smem)
     return e;
 }
 
+// a launch that may begin while the previous kernel on the stream is still running
+// (programmatic dependent launch; the kernel waits with pdl_wait_prev before its reads)
+template <typename... P, typename... A>
+static void launch_after(bool pdl, void (*k)(P...), int grid, int block, size_t smem, cudaStream_t st, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, static_cast<P>(args)...);
+}
+
 template <typename T>
 cudaError_t launch_boundary_batched(const BoundarySlot<T> *slots, const BatchIndex *idx, const size_t *smem, int s,
                                     cudaStream_t st) {
     if (idx[0].total()) k_rows_fwd_b<T><<<idx[0].total(), kBndThreads, smem[0], st>>>(slots, idx[0], s);
-    if (idx[1].total()) k_cols_b<T><<<idx[1].total(), kBndThreads, smem[1], st>>>(slots, idx[1], s);
-    if (idx[2].total()) k_rows_inv_b<T><<<idx[2].total(), kBndThreads, smem[2], st>>>(slots, idx[2], s);
-    if (idx[3].total()) k_bilinear_b<T><<<idx[3].total(), 256, 0, st>>>(slots, idx[3], s);
+    if (idx[1].total()) launch_after(true, k_cols_b<T>, idx[1].total(), kBndThreads, smem[1], st, slots, idx[1], s);
+    if (idx[2].total()) launch_after(true, k_rows_inv_b<T>, idx[2].total(), kBndThreads, smem[2], st, slots, idx[2], s);
+    if (idx[3].total()) launch_after(true, k_bilinear_b<T>, idx[3].total(), 256, (size_t)0, st, slots, idx[3], s);
     return cudaGetLastError();
 }
 
 template <typename T>
 void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
-                     StepGate gate, cudaStream_t st) {
+                     StepGate gate, cudaStream_t st, bool pdl) {
     k_rows_fwd<T><<<(g.M + 1) / 2, kBndThreads, smem_rows(bd, g.L), st>>>(bd, bz, tot, nch, g, gate);
-    k_cols<T><<<bd.H, kBndThreads, smem_cols(bd), st>>>(bd, gate);
-    k_rows_inv<T><<<bd.S, kBndThreads, smem_inv(bd), st>>>(bd, gate);
+    launch_after(pdl, k_cols<T>, bd.H, kBndThreads, smem_cols(bd), st, bd, gate);
+    launch_after(pdl, k_rows_inv<T>, bd.S, kBndThreads, smem_inv(bd), st, bd, gate);
     int n = (g.L + 1) * g.M + g.L * (g.M + 1);
-    k_bilinear<T><<<(n + 255) / 256, 256, 0, st>>>(bd, bx, by, g, gate);
+    launch_after(pdl, k_bilinear<T>, (n + 255) / 256, 256, (size_t)0, st, bd, bx, by, g, gate);
 }
 
 #define INST(T)                                                                                            \
     template size_t boundary_smem_need<T>(const BoundaryDev<T> &, int);                                   \
     template cudaError_t boundary_configure<T>(const BoundaryDev<T> &, int);                              \
     template void launch_boundary<T>(const BoundaryDev<T> &, const Geom &, const T *, const T *, int, T *, T *,  \
-                                     StepGate, cudaStream_t);                                             \
+                                     StepGate, cudaStream_t, bool);                                       \
     template BoundaryBlocks boundary_blocks<T>(const BoundaryDev<T> &, const Geom &);                     \
     template cudaError_t launch_boundary_batched<T>(const BoundarySlot<T> *, const BatchIndex *, const size_t *, int, \
                                                     cudaStream_t);                                        \

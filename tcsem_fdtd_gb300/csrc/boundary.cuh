@@ -82,9 +82,11 @@ struct BoundaryBlocks {
 namespace tcsem {
 template <typename T> size_t boundary_smem_need(const BoundaryDev<T> &bd, int L);
 template <typename T> cudaError_t boundary_configure(const BoundaryDev<T> &bd, int L);
+// pdl: the last three kernels may start while their predecessor finishes (programmatic
+// dependent launch); off where the chain runs beside a long sweep whose CTAs need the slots
 template <typename T>
 void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
-                     StepGate gate, cudaStream_t st);
+                     StepGate gate, cudaStream_t st, bool pdl = true);
 template <typename T> BoundaryBlocks boundary_blocks(const BoundaryDev<T> &bd, const Geom &g);
 // idx[4] and smem[3]: the block lists of rows_fwd, cols, rows_inv, bilinear and the largest shared memory
 template <typename T>

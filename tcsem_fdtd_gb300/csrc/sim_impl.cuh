@@ -191,6 +191,7 @@ template <typename T> struct SimImpl : SimBase {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool overlap = false;
+    bool overlap_pdl = false;  // programmatic dependent launch inside the boundary chain of the overlapped step
 
     ~SimImpl() override {
         for (auto &e : gexec) if (e) cudaGraphExecDestroy(e);
@@ -260,8 +261,42 @@ template <typename T> struct SimImpl : SimBase {
         }
         launches_per_step = 4 + (overlap ? 2 : 1) + 1;
         CK(cudaStreamSynchronize(stream));
+        if (overlap) choose_overlap_pdl();
         chunks_used = zc.n;
         top_used = overlap ? zc.kb[1] : 0;
+    }
+
+    // Beside the sweep, the boundary kernels launched early (programmatic dependent launch)
+    // take SM space that the sweep's single wave still needs when the sweep is the longer
+    // branch; they shorten the step when the boundary chain is the longer one.  Decided
+    // from one timed sweep and one timed boundary pass on the zero state (the choice
+    // changes timing only, never results).
+    void choose_overlap_pdl() {
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        auto timed = [&](auto &&fn) {
+            fn();  // untimed first launch
+            CK(cudaEventRecord(e0, stream));
+            fn();
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            return ms;
+        };
+        if (itx < 0) select(0);
+        const StepScalars<T> s = scal(sched.lam[0], sched.dt1[0], sched.dtB[0], 0.0);
+        const float t_sweep = timed([&] { sweep(0, s, nullptr, StepGate{nullptr, 0, 0}); });
+        const float t_bnd = timed([&] {
+            FieldSet<T> f = fs(0);
+            launch_boundary<T>(bd, g, f.bz, tot[0].as<T>(), zc.n, f.bx, f.by, StepGate{nullptr, 0, 0}, stream, false);
+        });
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        CK(cudaGetLastError());
+        overlap_pdl = t_bnd >= 0.5f * t_sweep;
+        zero_state();
     }
 
     // z-chunk layout: n chunks, the top one `top` planes deep (top <= 0: an even split)
@@ -618,7 +653,7 @@ template <typename T> struct SimImpl : SimBase {
         if (overlap) {  // fork: boundary -> top chunk on `side`, chunks 1.. on `stream`; join before the receivers
             CK(cudaEventRecord(ev_fork, stream));
             CK(cudaStreamWaitEvent(side, ev_fork, 0));
-            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, side);
+            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, side, overlap_pdl);
             sweep(b, StepScalars<T>{}, table, gate, 0, 1, side);
             sweep(b, StepScalars<T>{}, table, gate, 1, zc.n, stream);
             CK(cudaEventRecord(ev_join, side));
