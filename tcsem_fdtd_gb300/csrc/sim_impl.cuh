@@ -190,6 +190,10 @@ template <typename T> struct SimImpl : SimBase {
     // the boundary pipeline and the top z-chunk run on `side` beside the lower chunks
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the receivers of a step run on `rxs` beside the next step; ev_rx[b]: the last receiver
+    // launch that reads field set b has been enqueued
+    cudaStream_t rxs = nullptr;
+    cudaEvent_t ev_done = nullptr, ev_rx[2] = {nullptr, nullptr};
     bool overlap = false;
     bool overlap_pdl = false;  // programmatic dependent launch inside the boundary chain of the overlapped step
 
@@ -197,7 +201,10 @@ template <typename T> struct SimImpl : SimBase {
         for (auto &e : gexec) if (e) cudaGraphExecDestroy(e);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
+        if (ev_done) cudaEventDestroy(ev_done);
+        for (auto &e : ev_rx) if (e) cudaEventDestroy(e);
         if (side) cudaStreamDestroy(side);
+        if (rxs) cudaStreamDestroy(rxs);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -258,6 +265,9 @@ template <typename T> struct SimImpl : SimBase {
             CK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
             CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
             CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+            CK(cudaStreamCreateWithFlags(&rxs, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
+            for (auto &e : ev_rx) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
         launches_per_step = 4 + (overlap ? 2 : 1) + 1;
         CK(cudaStreamSynchronize(stream));
@@ -646,18 +656,38 @@ template <typename T> struct SimImpl : SimBase {
         begun = true;
     }
 
+    // Overlapped order: the receivers of step s (which read the field set step s wrote) run
+    // on `rxs` beside step s+1, which only reads that set; step s+2 rewrites it and waits for
+    // them.  A run of steps opens with both sets free and closes by joining `rxs` (the step
+    // counter advance comes after it).
+    void rx_open() {
+        if (overlap)
+            for (auto &e : ev_rx) CK(cudaEventRecord(e, stream));
+    }
+    void rx_close() {
+        if (overlap)
+            for (auto &e : ev_rx) CK(cudaStreamWaitEvent(stream, e, 0));
+    }
+
     // one step of main.cu:219-273 on the buffers starting at `b`
     void enqueue_step(int b, StepGate gate) {
         FieldSet<T> in = fs(b), out = fs(b ^ 1);
         const StepScalars<T> *table = steps.as<StepScalars<T>>();
-        if (overlap) {  // fork: boundary -> top chunk on `side`, chunks 1.. on `stream`; join before the receivers
+        if (overlap) {  // fork: boundary -> top chunk on `side`, chunks 1.. on `stream`; receivers on `rxs`
             CK(cudaEventRecord(ev_fork, stream));
             CK(cudaStreamWaitEvent(side, ev_fork, 0));
             launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, side, overlap_pdl);
+            CK(cudaStreamWaitEvent(side, ev_rx[b ^ 1], 0));  // set b^1 no longer read by older receivers
             sweep(b, StepScalars<T>{}, table, gate, 0, 1, side);
+            CK(cudaStreamWaitEvent(stream, ev_rx[b ^ 1], 0));
             sweep(b, StepScalars<T>{}, table, gate, 1, zc.n, stream);
             CK(cudaEventRecord(ev_join, side));
             CK(cudaStreamWaitEvent(stream, ev_join, 0));
+            CK(cudaEventRecord(ev_done, stream));
+            CK(cudaStreamWaitEvent(rxs, ev_done, 0));
+            launch_rx<T>(rd, out, tot[b ^ 1].as<T>(), zc, g, gate, RxAction{-1, 0, 0, -1, 0, 0}, rxs);
+            CK(cudaEventRecord(ev_rx[b ^ 1], rxs));
+            return;
         } else {
             launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, stream);
             sweep(b, StepScalars<T>{}, table, gate);
@@ -669,7 +699,9 @@ template <typename T> struct SimImpl : SimBase {
         if (gexec[b]) return gexec[b];
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        rx_open();
         for (int s = 0; s < gsteps; s++) enqueue_step(b ^ (s & 1), StepGate{gate_base.as<int>(), s, sched.nsteps});
+        rx_close();
         launch_advance(gate_base.as<int>(), gsteps, stream);
         cudaError_t e = cudaStreamEndCapture(stream, &graph);
         if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -690,8 +722,10 @@ template <typename T> struct SimImpl : SimBase {
         }
         // remainder: the same kernels launched one by one, gated on the same counter
         if (todo > 0) {
+            rx_open();
             for (long q = 0; q < todo; q++)
                 enqueue_step(cur ^ (int)(q & 1), StepGate{gate_base.as<int>(), (int)q, sched.nsteps});
+            rx_close();
             launch_advance(gate_base.as<int>(), (int)todo, stream);
             if (todo & 1) cur ^= 1;
             step += todo;
