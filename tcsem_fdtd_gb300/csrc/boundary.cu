@@ -36,28 +36,69 @@ constexpr int kBndThreads = 256;
 __device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait_prev() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-// Natural-spline second derivatives mb[0..n) of the line y[0..n) (stride ys)
-// from the precomputed elimination factors tab = g | w | inv | du; one thread
-// per line (n is at most 128).
+// Natural-spline second derivatives mb[0..n) of the line y[0..n) (stride ys) from
+// the precomputed elimination factors tab = g | w | inv | du (n values each): the
+// forward elimination of the tridiagonal system and the back substitution.
+// One warp solves a line: both sweeps are first-order linear recurrences,
+// rp_i = s_i - w_i rp_{i-1} forward and m_i = inv_i mb_i - inv_i du_i m_{i+1} backward,
+// so each lane composes the affine maps of a segment of at most ceil((n-2)/32)
+// nodes, a shuffle scan composes the segments, and each lane replays its segment
+// from its start value -- about 40 dependent steps instead of 2n.
 template <typename T>
-__device__ void spline_solve(const T *__restrict__ tab, int n, const T *y, int ys, T *mb) {
+__device__ void spline_solve_warp(const T *tab, int n, const T *y, int ys, T *mb) {
     const T *g = tab, *w = tab + n, *inv = tab + 2 * n, *du = tab + 3 * n;
-    T yc = y[ys], dprev = (yc - y[0]) * g[0], rp = T(0);
-    mb[0] = T(0);
-#pragma unroll 4
-    for (int i = 1; i < n - 1; i++) {
-        const T yn = y[(i + 1) * ys], dc = (yn - yc) * g[i];
-        rp = (dc - dprev) - w[i] * rp;
-        mb[i] = rp;
-        dprev = dc;
-        yc = yn;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, per = (n - 2 + 31) / 32;
+    const int i0 = 1 + lane * per, i1 = min(i0 + per, n - 1);  // this lane's unknowns [i0, i1)
+    auto fwd = [&](int i, T &a, T &b) {
+        a = -w[i];
+        b = (y[(i + 1) * ys] - y[i * ys]) * g[i] - (y[i * ys] - y[(i - 1) * ys]) * g[i - 1];
+    };
+    T A = T(1), B = T(0), a, b;
+    for (int i = i0; i < i1; i++) {
+        fwd(i, a, b);
+        B = a * B + b;
+        A = a * A;
     }
-    T m = T(0);
-    mb[n - 1] = m;
-#pragma unroll 4
-    for (int i = n - 2; i >= 1; i--) {
-        m = (mb[i] - du[i] * m) * inv[i];
-        mb[i] = m;
+    for (int off = 1; off < 32; off <<= 1) {  // maps of lanes <= this one, the earlier ones first
+        const T Ap = __shfl_up_sync(full, A, off), Bp = __shfl_up_sync(full, B, off);
+        if (lane >= off) {
+            B = A * Bp + B;
+            A = A * Ap;
+        }
+    }
+    T x = __shfl_up_sync(full, B, 1);  // rp at i0 - 1 (rp_0 = 0)
+    if (lane == 0) x = T(0);
+    for (int i = i0; i < i1; i++) {
+        fwd(i, a, b);
+        x = a * x + b;
+        mb[i] = x;
+    }
+    if (lane == 0) {
+        mb[0] = T(0);
+        mb[n - 1] = T(0);
+    }
+    __syncwarp();
+    A = T(1);
+    B = T(0);
+    for (int i = i1 - 1; i >= i0; i--) {
+        a = -inv[i] * du[i];
+        b = inv[i] * mb[i];
+        B = a * B + b;
+        A = a * A;
+    }
+    for (int off = 1; off < 32; off <<= 1) {  // maps of lanes >= this one, the later ones first
+        const T An = __shfl_down_sync(full, A, off), Bn = __shfl_down_sync(full, B, off);
+        if (lane + off < 32) {
+            B = A * Bn + B;
+            A = A * An;
+        }
+    }
+    x = __shfl_down_sync(full, B, 1);  // m at i1 (m_{n-1} = 0)
+    if (lane == 31) x = T(0);
+    for (int i = i1 - 1; i >= i0; i--) {
+        x = inv[i] * mb[i] - inv[i] * du[i] * x;
+        mb[i] = x;
     }
 }
 
@@ -195,9 +236,10 @@ __device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *
     if (!staged(bar, bd.err)) return;
     // left strip (Intep_BzIR2R_0x), core copy (Intep_BzIR2R_cpy_center), right strip (Intep_BzIR2R_1x)
     const T *r0 = row, *r1 = row + L;
-    if (threadIdx.x < 4) {
-        const StripPlan S = threadIdx.x < 2 ? R.s[0] : R.s[1];
-        spline_solve(tab + S.f, S.n, row + (threadIdx.x & 1) * L + S.src, 1, mbuf + threadIdx.x * R.nmax);
+    if (threadIdx.x < 128) {  // warps 0..3: strip (warp / 2) of row (warp & 1)
+        const int wq = threadIdx.x >> 5;
+        const StripPlan S = wq < 2 ? R.s[0] : R.s[1];
+        spline_solve_warp(tab + S.f, S.n, row + (wq & 1) * L + S.src, 1, mbuf + wq * R.nmax);
     }
     const int anl = bd.AnLx + bd.DL, AL = bd.AL;
     for (int c = threadIdx.x; c < bd.Nx; c += blockDim.x) a[anl + c] = {r0[AL + c], r1[AL + c]};
@@ -263,10 +305,11 @@ __device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
     if (!staged(bar, bd.err)) return;
     // front strip (Intep_BzIR2R_0y), core copy, back strip (Intep_BzIR2R_1y); the real and
     // imaginary parts of the column are independent lines
-    if (threadIdx.x < 4) {
-        const StripPlan S = threadIdx.x < 2 ? R.s[0] : R.s[1];
-        spline_solve(tab + S.f, S.n, reinterpret_cast<const T *>(col + S.src) + (threadIdx.x & 1), 2,
-                     mbuf + threadIdx.x * R.nmax);
+    if (threadIdx.x < 128) {  // warps 0..3: strip (warp / 2), real / imaginary part (warp & 1)
+        const int wq = threadIdx.x >> 5;
+        const StripPlan S = wq < 2 ? R.s[0] : R.s[1];
+        spline_solve_warp(tab + S.f, S.n, reinterpret_cast<const T *>(col + S.src) + (wq & 1), 2,
+                          mbuf + wq * R.nmax);
     }
     const int any = bd.Any + bd.DM, Ay = bd.Ay;
     for (int r = threadIdx.x; r < bd.Ny; r += blockDim.x) a[any + r] = col[Ay + r];
