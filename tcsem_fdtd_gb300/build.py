@@ -57,7 +57,7 @@ def build(verbose=False, jobs=None):
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + f".tmp{os.getpid()}"
-        subprocess.run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"], check=True)
+        subprocess.run([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"], check=True)
         os.replace(tmp, LIB)
     cli_obj = _compile("cli.cpp", verbose)
     if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(LIB), os.path.getmtime(cli_obj)):

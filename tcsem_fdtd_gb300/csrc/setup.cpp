@@ -108,12 +108,16 @@ SurveyInput read_survey_dir(const std::string &dir) {
     }
     long L = in.ALx2 + in.ALx1 + in.ARx2 + in.ARx1 + in.Nx, M = 2 * (in.Ay2 + in.Ay1) + in.Ny, N = in.Nz + in.Az2 + in.Az1;
     if (L < 1 || M < 1 || N < 1 || L * M * N > (1L << 33)) throw Error(TCSEM_ERR_INVALID, "bad grid dimensions");
-    {  // Cond.bin, float64 [N][M][L] (ModelingSetup.cpp:201-209)
-        std::string b = slurp(dir + "/Cond.bin", true);
-        size_t n = (size_t)L * M * N;
-        if (b.size() < n * sizeof(double)) throw Error(TCSEM_ERR_PARSE, "Cond.bin shorter than N*M*L doubles");
+    {  // Cond.bin, float64 [N][M][L] (ModelingSetup.cpp:201-209), read straight into place
+        const std::string path = dir + "/Cond.bin";
+        std::ifstream f(path, std::ios::binary | std::ios::ate);
+        if (!f) throw Error(TCSEM_ERR_IO, "cannot open " + path);
+        const size_t n = (size_t)L * M * N, bytes = (size_t)f.tellg();
+        if (bytes < n * sizeof(double)) throw Error(TCSEM_ERR_PARSE, "Cond.bin shorter than N*M*L doubles");
         in.con.resize(n);
-        std::memcpy(in.con.data(), b.data(), n * sizeof(double));
+        f.seekg(0);
+        if (!f.read(reinterpret_cast<char *>(in.con.data()), (std::streamsize)(n * sizeof(double))))
+            throw Error(TCSEM_ERR_IO, "cannot read " + path);
     }
     {  // LoadRxTxPos.cpp:51-84
         Tokens t(slurp(dir + "/Receiver.in"), "Receiver.in");

@@ -24,6 +24,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "boundary.cuh"
@@ -232,11 +233,20 @@ template <typename T> struct SimImpl : SimBase {
                 dev_bytes += vol;
                 CK(cudaMemsetAsync(fld[b][c].p, 0, vol, stream));
             }
-        {  // conductivity in the padded layout, plane -1 (air) and padding zero
+        {  // conductivity in the padded layout, plane -1 (air) and padding zero; planes split over threads
             std::vector<T> h((size_t)g.total(), T(0));
-            for (int k = 0; k < m.N; k++)
-                for (int j = 0; j < m.M; j++)
-                    for (int i = 0; i < m.L; i++) h[g.at(i, j, k)] = (T)m.in.con[((size_t)k * m.M + j) * m.L + i];
+            auto planes = [&](int k0, int k1) {
+                for (int k = k0; k < k1; k++)
+                    for (int j = 0; j < m.M; j++) {
+                        const double *src = m.in.con.data() + ((size_t)k * m.M + j) * m.L;
+                        T *dst = h.data() + g.at(0, j, k);
+                        for (int i = 0; i < m.L; i++) dst[i] = (T)src[i];
+                    }
+            };
+            const int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+            std::vector<std::thread> pool;
+            for (int q = 0; q < nt; q++) pool.emplace_back(planes, (int)((long)q * m.N / nt), (int)((long)(q + 1) * m.N / nt));
+            for (auto &th : pool) th.join();
             upload(con, h);
         }
         {  // axis tables
