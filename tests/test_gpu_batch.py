@@ -88,6 +88,21 @@ def test_slots_join_and_leave_between_blocks(built, case_dir):
         assert b.stats()["slots"] == 0
 
 
+def test_batch_with_the_padded_plane(built, case_dir):
+    """Slots carry the batch's options: a padded continuation plane (mode 2) gives the same
+    traces in the batch as alone."""
+    from tcsem_fdtd_gb300 import Batch, Simulation
+
+    dirs = [case_dir("small"), case_dir("cfg1")]
+    with Batch(precision=32, padded_plane=2) as b:
+        slots = [b.add(d) for d in dirs]
+        run_to_end(b)
+        for d, s in zip(dirs, slots):
+            with Simulation(d, precision=32, zchunks=1, padded_plane=2) as sim:
+                exp = sim.run(0)
+            assert rel_err(b.traces(s, nr=exp.shape[0]), exp) <= TOL[32], d
+
+
 def test_admission_by_device_budget(built, case_dir):
     from tcsem_fdtd_gb300 import Batch, TcsemError
 
