@@ -8,13 +8,13 @@ A :class:`Server` owns one device batch (tcsem_batch_* of include/tcsem.h).
 Each loop iteration (one graph block of the batch, `block` steps) it
 
 1. moves the requests whose arrival time has passed into the queue,
-2. admits queued requests in arrival order while the batch accepts them --
-   a request is accepted when the estimate of its device footprint fits the
-   remaining budget (the batch refuses it otherwise, nothing allocated), so
-   admission is by HBM footprint and a large request waits until enough
-   finished requests have left,
-3. enqueues one block of steps for every running request (asynchronous: the
-   host prepares the next admissions while the GPU runs it),
+2. enqueues one block of steps for every running request (asynchronous),
+3. while the GPU runs that block, admits queued requests in arrival order
+   while the batch accepts them -- a request is accepted when the estimate of
+   its device footprint fits the remaining budget (the batch refuses it
+   otherwise, nothing allocated), so admission is by HBM footprint and a large
+   request waits until enough finished requests have left; reading its input
+   files and setting up its device state overlap the running block,
 4. collects finished requests (traces copied to the host, slot freed).
 
 Requests join and leave only at block boundaries; each request's fields stay on
@@ -77,10 +77,11 @@ class Server:
 
     def step(self, now):
         """One loop iteration; returns the requests that finished in it."""
+        if self.running:
+            self.batch.advance(self.block)  # the new admissions below overlap this block
         self._admit(now)
         if not self.running:
             return []
-        self.batch.advance(self.block)
         finished = []
         for slot in self.batch.poll():
             req = self.running.pop(slot)
