@@ -48,7 +48,9 @@ typedef struct {
     int device;           /* CUDA device ordinal, default 0 */
     int fix_dual_bipole;  /* 1: inject the second bipole of ort=5 at its own cells (default 0 = as the reference) */
     int graph_steps;      /* steps per captured CUDA graph, 0 = default (even numbers only) */
-    int zchunks;          /* z-chunks of the fused sweep, 0 = chosen from the grid and the GPU */
+    int zchunks;          /* z-chunks of the fused sweep, 0 = chosen from the grid and the GPU,
+                             -1 = the fastest of the layouts near that choice, timed at open
+                             (the last bits of the traces may then differ between runs) */
     int serial_boundary;  /* 1: boundary pipeline strictly before the whole sweep; default 0 = the
                              boundary and the top z-chunk run beside the lower chunks */
     int top_planes;       /* planes of the top z-chunk, 0 = default (one plane beside the boundary, so

@@ -282,6 +282,7 @@ template <typename T> struct SimImpl : SimBase {
         launches_per_step = 4 + (overlap ? 2 : 1) + 1;
         CK(cudaStreamSynchronize(stream));
         if (overlap) choose_overlap_pdl();
+        if (overlap && opts.zchunks < 0 && sched.nsteps >= 64) tune_layout();
         chunks_used = zc.n;
         top_used = overlap ? zc.kb[1] : 0;
     }
@@ -317,6 +318,49 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaGetLastError());
         overlap_pdl = t_bnd >= 0.5f * t_sweep;
         zero_state();
+    }
+
+    // The layout autotuner (tcsem_opts.zchunks = -1): times a captured block of 8 steps for
+    // each layout near the rule of init_chunks -- one to five lower chunks around it, a
+    // one-plane or an even top chunk -- and keeps the fastest.  The Bz prefix is summed per
+    // chunk, so the layout decides the order of some FP additions: with the tuner the last
+    // bits may differ between runs whose timings chose differently.
+    int rule_lower = 1;  // lower chunks the rule of init_chunks chose
+    void tune_layout() {
+        if (itx < 0) select(0);
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        struct Cand { int n, top; };
+        std::vector<Cand> cands;
+        for (int lower = std::max(1, rule_lower - 2); lower <= rule_lower + 2 && lower + 1 <= max_chunks(); lower++)
+            for (int top : {1, 0}) cands.push_back({lower + 1, top});
+        const int keep = gsteps;
+        gsteps = 8;
+        float best = 1e30f;
+        Cand pick = {zc.n, zc.n > 1 && zc.kb[1] == 1 ? 1 : 0};
+        for (const Cand &c : cands) {
+            set_chunks(c.n, c.top);
+            for (auto &e : gexec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+            zero_state();
+            cudaGraphExec_t ge = graph_for(cur);
+            CK(cudaGraphLaunch(ge, stream));  // untimed
+            CK(cudaEventRecord(e0, stream));
+            CK(cudaGraphLaunch(ge, stream));
+            CK(cudaGraphLaunch(ge, stream));
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) { best = ms; pick = c; }
+        }
+        gsteps = keep;
+        for (auto &e : gexec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        set_chunks(pick.n, pick.top);
+        zero_state();
+        CK(cudaStreamSynchronize(stream));
     }
 
     // z-chunk layout: n chunks, the top one `top` planes deep (top <= 0: an even split)
@@ -355,10 +399,13 @@ template <typename T> struct SimImpl : SimBase {
             top = 1;
         }
         n = std::min(n, max_chunks());
+        rule_lower = n - 1;
         if (opts.zchunks > 0) n = std::min(std::min(opts.zchunks, kMaxChunks), m.N);
         if (opts.top_planes != 0) top = opts.top_planes;  // > 0: that many planes, < 0: an even split
         set_chunks(n, top);
-        const size_t tb = (size_t)n * g.PS * sizeof(T);
+        // the autotuner may pick up to two more lower chunks than the rule
+        const int nalloc = opts.zchunks < 0 ? std::max(n, std::min(rule_lower + 3, max_chunks())) : n;
+        const size_t tb = (size_t)nalloc * g.PS * sizeof(T);
         for (int b = 0; b < 2; b++) {
             tot[b].alloc(tb);
             dev_bytes += tb;

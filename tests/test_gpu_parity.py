@@ -158,6 +158,15 @@ def test_full_run_fp64_matches_oracle(built, case_dir, name, zchunks):
     assert trace_error(got, exp) < 1e-8
 
 
+def test_layout_autotuner_fp64(built, case_dir):
+    """zchunks = -1 times layouts near the rule at open and keeps one; whichever it keeps, the
+    traces still match the oracle."""
+    sim, orc = pair(case_dir, "small", 64, zchunks=-1)
+    assert 2 <= sim.info["zchunks"] <= 16 and sim.info["top_planes"] >= 1
+    exp, _ = orc.run(0)
+    assert trace_error(sim.run(0, nr=exp.shape[0]), exp) < 1e-8
+
+
 @pytest.mark.parametrize("name", ["tiny", "small"])
 def test_full_run_fp32_within_one_percent(built, case_dir, name):
     sim, orc = pair(case_dir, name, 32)
