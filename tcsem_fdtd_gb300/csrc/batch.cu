@@ -58,6 +58,12 @@ template <typename T> struct BatchImpl : BatchBase {
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 64;
     bool dirty = true;
+    // layout autotuner (opts.zchunks = -1): at the first advance every slot's z-chunk layout
+    // is timed for a few candidates on one graph block and the fastest is kept, also for
+    // slots added later
+    static constexpr int kTuneChunks = 3;
+    bool tune_pending = false;
+    int lay_n = 1, lay_top = 0;
 
     ~BatchImpl() override {
         if (stream) cudaStreamSynchronize(stream);
@@ -86,6 +92,7 @@ template <typename T> struct BatchImpl : BatchBase {
         }
         gsteps = opts.graph_steps > 0 ? opts.graph_steps : 64;
         if (gsteps % 2) gsteps++;
+        tune_pending = opts.zchunks < 0;
     }
 
     Slot &find(int id) {
@@ -99,8 +106,10 @@ template <typename T> struct BatchImpl : BatchBase {
         auto sim = std::make_unique<SimImpl<T>>();
         sim->opts = opts;
         // the slots fill the GPU together: one z-chunk each unless set (no halo planes; the
-        // boundary kernels of all slots run as wide launches before the sweep)
+        // boundary kernels of all slots run as wide launches before the sweep) or tuned
+        const bool tuned = opts.zchunks < 0;
         if (sim->opts.zchunks <= 0) sim->opts.zchunks = 1;
+        if (tuned) sim->tot_chunks_min = kTuneChunks;
         sim->device = device;
         sim->model.build(read_survey_dir(dir));
         sim->sched = sim->model.schedule();
@@ -109,6 +118,7 @@ template <typename T> struct BatchImpl : BatchBase {
             throw Error(TCSEM_ERR_NOMEM, "device budget: the survey needs about " + std::to_string(est) +
                                              " bytes, " + std::to_string(budget - std::min(budget, used)) + " are free");
         sim->init();
+        if (tuned && !tune_pending) sim->set_chunks(std::min(lay_n, sim->max_chunks()), lay_top);
         sim->begin(itx);
         CK(cudaStreamSynchronize(sim->stream));
         Slot s;
@@ -198,7 +208,54 @@ template <typename T> struct BatchImpl : BatchBase {
         if (e != cudaSuccess) throw Error(TCSEM_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e));
     }
 
+    // time one graph block of 8 steps per candidate layout on the slots as admitted, then put
+    // every slot back to its zero state at step 0 with the fastest layout
+    void tune() {
+        struct Cand { int n, top; };
+        const Cand cands[] = {{1, 0}, {2, 0}, {2, 1}, {3, 0}, {3, 1}};
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        float best = 1e30f;
+        Cand pick = cands[0];
+        auto layout = [&](const Cand &c) {
+            CK(cudaStreamSynchronize(stream));
+            for (auto &s : slots) {
+                s.sim->set_chunks(std::min(c.n, s.sim->max_chunks()), c.top);
+                s.sim->zero_state();  // the slot's transmitter stays selected
+                CK(cudaStreamSynchronize(s.sim->stream));
+                s.done = 0;
+            }
+            dirty = true;
+        };
+        const int keep = gsteps;
+        gsteps = 8;
+        for (const Cand &c : cands) {
+            layout(c);
+            rebuild();
+            if (running.empty()) break;
+            CK(cudaGraphLaunch(gexec, stream));  // untimed
+            CK(cudaEventRecord(e0, stream));
+            CK(cudaGraphLaunch(gexec, stream));
+            CK(cudaEventRecord(e1, stream));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) { best = ms; pick = c; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        gsteps = keep;
+        lay_n = pick.n;
+        lay_top = pick.top;
+        layout(pick);
+    }
+
     void advance(long nsteps) override {
+        if (tune_pending && !slots.empty()) {
+            tune_pending = false;
+            tune();
+        }
         if (dirty) rebuild();
         if (running.empty()) return;
         for (long k = 0; k < nsteps; k += gsteps) {
@@ -234,6 +291,9 @@ template <typename T> struct BatchImpl : BatchBase {
             o->precision = s.sim->opts.precision;
             o->device_bytes = s.bytes;
             o->launches_per_step = 7;
+            const ZChunks &zc = s.sim->zc;
+            o->zchunks = zc.n;
+            o->top_planes = zc.n > 1 && zc.kb[1] != (int)(s.sim->model.N / zc.n) ? zc.kb[1] : 0;
         }
         if (steps_done) *steps_done = s.done;
     }

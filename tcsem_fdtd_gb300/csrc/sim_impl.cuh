@@ -113,6 +113,7 @@ struct SimBase {
     size_t dev_bytes = 0;
     int launches_per_step = 0;
     int chunks_used = 0, top_used = 0;  // z-chunk layout of the sweep in use (top_used 0: an even split)
+    int tot_chunks_min = 0;             // chunk totals to allocate room for at least (a batch's tuner)
     virtual ~SimBase() {}
     virtual void init() = 0;
     virtual void select(int itx) = 0;
@@ -404,7 +405,8 @@ template <typename T> struct SimImpl : SimBase {
         if (opts.top_planes != 0) top = opts.top_planes;  // > 0: that many planes, < 0: an even split
         set_chunks(n, top);
         // the autotuner may pick up to two more lower chunks than the rule
-        const int nalloc = opts.zchunks < 0 ? std::max(n, std::min(rule_lower + 3, max_chunks())) : n;
+        int nalloc = opts.zchunks < 0 ? std::max(n, std::min(rule_lower + 3, max_chunks())) : n;
+        nalloc = std::max(nalloc, std::min(tot_chunks_min, max_chunks()));
         const size_t tb = (size_t)nalloc * g.PS * sizeof(T);
         for (int b = 0; b < 2; b++) {
             tot[b].alloc(tb);

@@ -103,6 +103,27 @@ def test_batch_with_the_padded_plane(built, case_dir):
             assert rel_err(b.traces(s, nr=exp.shape[0]), exp) <= TOL[32], d
 
 
+def test_batch_layout_autotuner(built, case_dir):
+    """zchunks = -1: the batch times a few z-chunk layouts on its first block, restarts the
+    slots and keeps the fastest; each slot's traces equal the survey run alone with the
+    layout the slot reports."""
+    from tcsem_fdtd_gb300 import Batch
+
+    dirs = [case_dir("small"), case_dir("tiny"), case_dir("cfg1")]
+    with Batch(precision=32, zchunks=-1) as b:
+        slots = [b.add(d) for d in dirs]
+        run_to_end(b)
+        for d, s in zip(dirs, slots):
+            info = b.info(s)
+            assert 1 <= info["zchunks"] <= 3
+            top = info["top_planes"] if info["top_planes"] > 0 else -1
+            from tcsem_fdtd_gb300 import Simulation
+
+            with Simulation(d, precision=32, zchunks=info["zchunks"], top_planes=top) as sim:
+                exp = sim.run(0)
+            assert rel_err(b.traces(s, nr=exp.shape[0]), exp) <= TOL[32], (d, info["zchunks"], top)
+
+
 def test_admission_by_device_budget(built, case_dir):
     from tcsem_fdtd_gb300 import Batch, TcsemError
 
