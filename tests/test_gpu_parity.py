@@ -303,6 +303,23 @@ def test_overlapped_boundary_equals_serial_order(built, case_dir, precision):
         np.testing.assert_array_equal(runs[0], runs[1])
 
 
+def test_cli_smooth_plane_flag(built, case_dir, tmp_path):
+    """tcsem_fdtd --smooth-plane writes what Simulation(padded_plane=2) computes."""
+    import shutil
+
+    from tcsem_fdtd_gb300 import Simulation, build
+
+    d = tmp_path / "run"
+    shutil.copytree(case_dir("small"), d)
+    r = subprocess.run([build.CLI, str(d), "--smooth-plane"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = open(d / "Tx1.bout", "rb").read()
+    hdr = np.frombuffer(raw[:12], np.int32)
+    data = np.frombuffer(raw[12:], np.float64).reshape(hdr)
+    with Simulation(case_dir("small"), precision=32, padded_plane=2) as sim:
+        np.testing.assert_array_equal(data, sim.run(0, nr=int(hdr[0])))
+
+
 def test_cli_writes_reference_formats(built, case_dir, tmp_path):
     import shutil
 
