@@ -2,12 +2,15 @@
 
     python -m tcsem_fdtd_gb300.profile_steps [--workload cfg3] [--steps 16]
                                              [--precision 32] [--serial-boundary] [--fused N]
+                                             [--batch N]
 
 Writes the workload's input files to a temporary directory, opens it through
 the C ABI and advances `--steps` steps (CUDA graphs of 8 steps), then exits.
 With `--fused N` it instead launches the fused sweep alone N times
 (tcsem_fused_step: every z-chunk of the default layout in one launch, the
-launch bench.py times for the roofline).
+launch bench.py times for the roofline).  With `--batch N` it advances a
+batch of the first N generated surveys of the batched workload instead
+(`--steps` steps, graph blocks of 8).
 It reports nothing about speed: time with bench.py, and use this under ncu to
 get a launch list or a capture of one kernel on a short run.
 """
@@ -29,7 +32,24 @@ def main(argv=None):
     ap.add_argument("--serial-boundary", action="store_true",
                     help="boundary pipeline before one launch of the whole sweep (no overlap)")
     ap.add_argument("--fused", type=int, default=0, help="launch the fused sweep alone this many times")
+    ap.add_argument("--batch", type=int, default=0, help="advance a batch of this many generated surveys")
     a = ap.parse_args(argv)
+    if a.batch:
+        from tcsem_fdtd_gb300 import Batch
+
+        root = tempfile.mkdtemp(prefix="tcsem_prof_batch_")
+        dirs = []
+        for q in range(a.batch):
+            dq = os.path.join(root, f"s{q:03d}")
+            inputs.write_case(inputs.batch_case(q), dq)
+            dirs.append(dq)
+        with Batch(precision=a.precision, graph_steps=8) as b:
+            for dq in dirs:
+                b.add(dq)
+            b.advance(a.steps)
+            b.poll()
+        print(f"batch of {a.batch}: {a.steps} steps", flush=True)
+        return 0
     d = tempfile.mkdtemp(prefix=f"tcsem_prof_{a.workload}_")
     inputs.write_case(inputs.case(a.workload), d)
     with Simulation(d, precision=a.precision, graph_steps=8, serial_boundary=a.serial_boundary) as sim:
