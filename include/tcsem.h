@@ -196,6 +196,14 @@ tcsem_status tcsem_batch_stats(tcsem_batch_t *batch, int *slots, int *running, s
 #define TCSEM_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
 tcsem_status tcsem_upcontinuation_noalloc(tcsem_sim_t *sim);
 
+/* Self-test of the bounded waits every kernel uses on its bulk copies (no
+ * counterpart in the reference): one CTA on `device` waits on an mbarrier that
+ * nothing completes, gives up after `polls` polls and records that in a device
+ * error word, read back into *gave_up (1 when the wait gave up).  The device
+ * stays usable afterwards.  A production kernel that gives up the same way
+ * makes the next synchronising call on its handle return TCSEM_ERR_CUDA. */
+tcsem_status tcsem_selftest_bounded_wait(int device, int polls, int *gave_up);
+
 #ifdef __cplusplus
 }
 #endif

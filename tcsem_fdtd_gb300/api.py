@@ -85,6 +85,7 @@ def library():
         "tcsem_get_schedule": (i, [vp, dp, dp, dp, dp, l_]),
         "tcsem_time_steps": (i, [vp, i, l_, dp, dp, dp]),
         "tcsem_timed_advance": (i, [vp, l_, dp]),
+        "tcsem_selftest_bounded_wait": (i, [i, i, ip]),
     }
     sig.update({
         "tcsem_batch_create": (i, [C.POINTER(Opts), C.c_size_t, C.POINTER(vp)]),
@@ -105,6 +106,15 @@ def library():
         f.argtypes = args
     _lib = L
     return L
+
+
+def selftest_bounded_wait(device=0, polls=1000):
+    """tcsem_selftest_bounded_wait: 1 when a wait on an mbarrier that nothing completes gave up."""
+    g = C.c_int(0)
+    st = library().tcsem_selftest_bounded_wait(device, polls, C.byref(g))
+    if st != 0:
+        raise TcsemError(st, "bounded-wait self-test failed")
+    return g.value
 
 
 def _dptr(a):

@@ -28,9 +28,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait: gives up after ~1e6 polls (each poll may suspend for a while)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
-    for (int it = 0; it < (1 << 20); it++)
+// bounded wait: gives up after `polls` polls, ~1e6 by default (each poll may suspend for a while)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, int polls = 1 << 20) {
+    for (int it = 0; it < polls; it++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -15,6 +15,8 @@
 // and leave (tcsem_batch_remove) between graph launches, which rebuilds the
 // tables and re-captures the graph.  Admission is by device memory: a slot is
 // accepted when the estimate of its allocation fits in the batch's budget.
+#include <nvtx3/nvToolsExt.h>
+
 #include "sim_impl.cuh"
 
 namespace tcsem {
@@ -407,6 +409,8 @@ tcsem_status tcsem_batch_destroy(tcsem_batch_t *b) {
 }
 
 tcsem_status tcsem_batch_add(tcsem_batch_t *b, const char *dir, int itx, int *slot) {
+    nvtxRangePushA("tcsem_batch_add");
+    struct Pop { ~Pop() { nvtxRangePop(); } } pop;
     if (!dir) return TCSEM_ERR_INVALID;
     return bguard(b, [&](BatchBase &x) {
         const int id = x.add(dir, itx);
@@ -415,6 +419,8 @@ tcsem_status tcsem_batch_add(tcsem_batch_t *b, const char *dir, int itx, int *sl
 }
 
 tcsem_status tcsem_batch_advance(tcsem_batch_t *b, long nsteps) {
+    nvtxRangePushA("tcsem_batch_advance");
+    struct Pop { ~Pop() { nvtxRangePop(); } } pop;
     return bguard(b, [&](BatchBase &x) { x.advance(nsteps); });
 }
 

@@ -2,7 +2,33 @@
 // batch.cu); the simulation state itself is in sim_impl.cuh.
 #include <mutex>
 
+#include <nvtx3/nvToolsExt.h>
+
+#include "async.cuh"
 #include "sim_impl.cuh"
+
+namespace tcsem {
+// NVTX range over one entry point (visible in Nsight tools, free without one attached)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
+// One CTA waits on an mbarrier that nothing completes: every thread gives up after `polls`
+// polls and the CTA records it in the error word, as the production kernels do when a
+// bulk copy does not arrive.
+__global__ void k_wait_selftest(int *err, int polls) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0u, polls);
+    __syncthreads();
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+}
+}  // namespace tcsem
 
 // ================================================================== C ABI
 using namespace tcsem;
@@ -40,6 +66,7 @@ void tcsem_default_opts(tcsem_opts *o) {
 }
 
 tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t **out) {
+    NvtxRange nr("tcsem_open_dir");
     if (!dir || !out) { g_open_err = "null argument"; return TCSEM_ERR_INVALID; }
     *out = nullptr;
     tcsem_opts o;
@@ -102,7 +129,10 @@ tcsem_status tcsem_get_info(const tcsem_sim_t *s, tcsem_info *o) {
 }
 
 tcsem_status tcsem_begin(tcsem_sim_t *s, int itx) { return guard(s, [&](SimBase &b) { b.begin(itx); }); }
-tcsem_status tcsem_advance(tcsem_sim_t *s, long n, int *done) { return guard(s, [&](SimBase &b) { b.advance(n, done); }); }
+tcsem_status tcsem_advance(tcsem_sim_t *s, long n, int *done) {
+    NvtxRange nr("tcsem_advance");
+    return guard(s, [&](SimBase &b) { b.advance(n, done); });
+}
 tcsem_status tcsem_get_traces(tcsem_sim_t *s, double *t) {
     return guard(s, [&](SimBase &b) {
         if (!t) throw Error(TCSEM_ERR_INVALID, "null trace buffer");
@@ -117,6 +147,7 @@ tcsem_status tcsem_synchronize(tcsem_sim_t *s) {
     });
 }
 tcsem_status tcsem_run(tcsem_sim_t *s, int itx, double *t) {
+    NvtxRange nr("tcsem_run");
     return guard(s, [&](SimBase &b) {
         if (!t) throw Error(TCSEM_ERR_INVALID, "null trace buffer");
         b.begin(itx);
@@ -124,6 +155,25 @@ tcsem_status tcsem_run(tcsem_sim_t *s, int itx, double *t) {
         b.advance(b.sched.nsteps, &done);
         b.traces(t);
     });
+}
+
+tcsem_status tcsem_selftest_bounded_wait(int device, int polls, int *gave_up) {
+    if (!gave_up || polls < 1) return TCSEM_ERR_INVALID;
+    *gave_up = 0;
+    int *err = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess || cudaMalloc(&err, sizeof(int)) != cudaSuccess) return TCSEM_ERR_CUDA;
+    tcsem_status st = TCSEM_OK;
+    int h = 0;
+    if (cudaMemset(err, 0, sizeof(int)) != cudaSuccess) st = TCSEM_ERR_CUDA;
+    if (st == TCSEM_OK) {
+        k_wait_selftest<<<1, 64>>>(err, polls);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+            cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = TCSEM_ERR_CUDA;
+    }
+    cudaFree(err);
+    *gave_up = h;
+    return st;
 }
 
 tcsem_status tcsem_write_bout(tcsem_sim_t *s, int itx, const double *t, const char *path) {
