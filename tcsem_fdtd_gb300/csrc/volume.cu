@@ -125,8 +125,9 @@ void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, cu
 // One pass per time step over the volume: old E/B/sigma planes stream into a
 // shared-memory ring through TMA bulk-tensor copies (cp.async.bulk.tensor,
 // mbarrier completion), the new E and B go to the other buffer of the
-// ping-pong pair.  Tiles are 32 x 8 columns, aligned so every TMA box starts
-// on a 16-byte boundary; one thread per column marches z bottom-up through one
+// ping-pong pair.  Tiles are 64 x 8 columns, aligned so every TMA box starts
+// on a 16-byte boundary; each thread owns two columns of a row (x = lane and
+// lane + 32) and marches them z bottom-up through one
 // z-chunk.  Warps 0..7 own the tile rows, warp 8 recomputes the +y halo row
 // and warp 9 the +x halo column (E and the B components the tile's Bz needs),
 // so no CTA waits for another; the -x/-y halo is plain old data in the TMA box.
