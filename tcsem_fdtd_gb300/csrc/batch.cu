@@ -57,6 +57,7 @@ template <typename T> struct BatchImpl : BatchBase {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     size_t smem_bnd[3] = {0, 0, 0};
     int nmax = 0;
+    int lps = 6;  // launches per step for all slots (a seventh when some slot has lower z-chunks)
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 64;
     bool dirty = true;
@@ -181,6 +182,7 @@ template <typename T> struct BatchImpl : BatchBase {
         }
         CK(cudaMemcpy(counters.p, hc.data(), kMaxSlots * sizeof(int), cudaMemcpyHostToDevice));
         dirty = false;
+        lps = 6 + (ilow.total() > 0 ? 1 : 0);
         if (!n) return;
         CK(sweep_configure<T>(nmax));
         CK(boundary_configure_batched<T>(smem_bnd));
@@ -292,7 +294,7 @@ template <typename T> struct BatchImpl : BatchBase {
             o->nsteps = s.sim->sched.nsteps;
             o->precision = s.sim->opts.precision;
             o->device_bytes = s.bytes;
-            o->launches_per_step = 7;
+            o->launches_per_step = lps;
             const ZChunks &zc = s.sim->zc;
             o->zchunks = zc.n;
             o->top_planes = zc.n > 1 && zc.kb[1] != (int)(s.sim->model.N / zc.n) ? zc.kb[1] : 0;
