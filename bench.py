@@ -1,6 +1,6 @@
 """Benchmark of the TCSEM_FDTD time-stepping hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload cfg3]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload marine3d_256x256x160]
 
 A "step" is one time step of the hot path (boundary pipeline, fused E/B
 sweep, receiver sampling) over the workload's whole grid; the metric is
@@ -10,8 +10,8 @@ input formats).  With N > 1 (torchrun) every rank runs an independent replica
 on its own GPU; the time is the maximum over ranks and the value the sum of
 cells*steps over ranks.
 
---workload cfg4 runs 64 generated surveys as one device batch and one at a
-time (simulations per hour); --workload cfg5 serves a seeded Poisson stream of
+--workload batch64 runs 64 generated surveys as one device batch and one at a
+time (simulations per hour); --workload serve_poisson serves a seeded Poisson stream of
 requests with continuous batching and one at a time (sims/hr, p50/p99).
 
 --impl reference times the CPU implementation of the same path (the FP64 C
@@ -199,13 +199,13 @@ def run_reference_arm(args, dist):
 
 
 def run_batch_workloads(args, dist):
-    """cfg4: generated surveys advanced as one device batch vs one at a time (sims/hr).
-    cfg5: a seeded Poisson stream of requests served with continuous batching (sims/hr, p50/p99)."""
+    """batch64: generated surveys advanced as one device batch vs one at a time (sims/hr).
+    serve_poisson: a seeded Poisson stream of requests served with continuous batching (sims/hr, p50/p99)."""
     from tcsem_fdtd_gb300 import Batch, Simulation, build, inputs
     from tcsem_fdtd_gb300 import serve as sv
 
     build.build()
-    if args.workload == "cfg5":
+    if args.workload == "serve_poisson":
         reqs = sv.make_stream(args.surveys, args.rate, 5 + dist.rank, tn=(1.0, 10.0))
         srv = sv.Server(budget=64 << 30, block=64)
         try:
@@ -217,13 +217,13 @@ def run_batch_workloads(args, dist):
         line = {"metric": "sims/hr", "value": dist.reduce(batched["sims_per_hour"], "sum"), "unit": "sims/hr",
                 "n_gpus": dist.world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic", "impl": "gb300",
-                "config": {"workload": "cfg5", "requests": args.surveys, "rate_per_s": args.rate,
+                "config": {"workload": "serve_poisson", "requests": args.surveys, "rate_per_s": args.rate,
                            "sizes": "64x64x48 .. 256x256x160", "windows_s": [1.0, 10.0], "budget_gb": 64},
                 "batched": batched, "plain": plain, "vs_plain": batched["sims_per_hour"] / plain["sims_per_hour"]}
         if dist.rank == 0:
             print(json.dumps(line), flush=True)
         return 0
-    root = tempfile.mkdtemp(prefix="tcsem_bench_cfg4_")
+    root = tempfile.mkdtemp(prefix="tcsem_bench_batch64_")
     dirs = []
     for q in range(args.surveys):
         d = os.path.join(root, f"s{q:03d}")
@@ -252,7 +252,7 @@ def run_batch_workloads(args, dist):
     line = {"metric": "sims/hr", "value": 3600.0 * n_all / tb_max, "unit": "sims/hr", "n_gpus": dist.world,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic", "impl": "gb300",
-            "config": {"workload": "cfg4", "surveys": len(dirs), "grids": "96..192 x 96..192 x 96..128",
+            "config": {"workload": "batch64", "surveys": len(dirs), "grids": "96..192 x 96..192 x 96..128",
                        "window_s": 1.0, "what": "tcsem_batch_add of every survey, all steps, traces to host"},
             "batched_s": tb, "plain_s": tp, "plain_sims_per_hour": 3600.0 * len(dirs) / tp,
             "vs_plain": tp / tb,
@@ -268,18 +268,18 @@ def main():
     ap.add_argument("--steps", type=int, default=2048)
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="cfg3")
+    ap.add_argument("--workload", default="marine3d_256x256x160")
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--surveys", type=int, default=64, help="cfg4: surveys in the batch; cfg5: requests")
-    ap.add_argument("--rate", type=float, default=8.0, help="cfg5: mean request arrivals per second")
+    ap.add_argument("--surveys", type=int, default=64, help="batch64: surveys in the batch; serve_poisson: requests")
+    ap.add_argument("--rate", type=float, default=8.0, help="serve_poisson: mean request arrivals per second")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     dist = Dist()
     try:
         if args.impl == "reference":
             return run_reference_arm(args, dist)
-        if args.workload in ("cfg4", "cfg5"):
+        if args.workload in ("batch64", "serve_poisson"):
             return run_batch_workloads(args, dist)
         return run_gb300(args, dist)
     finally:

@@ -268,7 +268,7 @@ CASES = {
         transmitters=[dict(ort=1, len=200.0, x=0.0, y=0.0, z=600.0)],
     ),
     # survey config 1: homogeneous 1 S/m half-space, 64 x 64 x 48, 25 m, growth 1.15
-    "cfg1": _base(
+    "halfspace_64x64x48": _base(
         dmin=(25.0, 25.0, 25.0), arg1=1.15, arg2=1.15, xsplit=(0, 12, 24, 28, 0), ysplit=(0, 20, 24),
         zsplit=(0, 28, 20), n1=200, sita_t=1e-5, sfa1=1.5, sfa2=2.0, T0=1e-4, Tn=1.0, Nt=61,
         comps=(1, 1, 0, 0, 1, 1), model=dict(kind="uniform", sigma=1.0),
@@ -286,7 +286,7 @@ CASES = {
         transmitters=[dict(ort=1, len=25.0, x=0.0, y=0.0, z=0.0)],
     ),
     # survey config 2: 1-D marine model, 128 x 128 x 96 at 20 m
-    "cfg2": _base(
+    "marine1d_128x128x96": _base(
         dmin=(20.0, 20.0, 20.0), arg1=1.06, arg2=1.15, xsplit=(6, 14, 48, 50, 10), ysplit=(6, 14, 88),
         zsplit=(10, 30, 56), n1=200, sita_t=1e-4, sfa1=2.0, sfa2=2.0, T0=1e-3, Tn=10.0, Nt=81,
         comps=(1, 1, 0, 1, 1, 1),
@@ -295,7 +295,7 @@ CASES = {
         transmitters=[dict(ort=1, len=40.0, x=0.0, y=0.0, z=950.0)],
     ),
     # survey config 3: 3-D marine model, 256 x 256 x 160 at 25 m
-    "cfg3": _base(
+    "marine3d_256x256x160": _base(
         dmin=(25.0, 25.0, 25.0), arg1=1.08, arg2=1.08, xsplit=(0, 40, 176, 40, 0), ysplit=(0, 40, 176),
         zsplit=(0, 60, 100), n1=200, sita_t=1e-4, sfa1=2.0, sfa2=2.0, T0=1e-3, Tn=10.0, Nt=81,
         comps=(1, 1, 0, 1, 1, 1),

@@ -1,6 +1,6 @@
 """Run a few time steps of a named synthetic workload, for profilers.
 
-    python -m tcsem_fdtd_gb300.profile_steps [--workload cfg3] [--steps 16]
+    python -m tcsem_fdtd_gb300.profile_steps [--workload marine3d_256x256x160] [--steps 16]
                                              [--precision 32] [--serial-boundary] [--fused N]
                                              [--batch N]
 
@@ -26,7 +26,7 @@ def main(argv=None):
     from tcsem_fdtd_gb300 import Simulation, inputs
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="cfg3")
+    ap.add_argument("--workload", default="marine3d_256x256x160")
     ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--serial-boundary", action="store_true",

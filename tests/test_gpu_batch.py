@@ -49,7 +49,7 @@ def run_to_end(b, block=64, limit=100000):
 def test_batch_equals_each_survey_alone(built, case_dir, precision):
     from tcsem_fdtd_gb300 import Batch
 
-    cases = [("tiny", 0), ("small", 0), ("txvar", 3), ("cfg1", 0)]
+    cases = [("tiny", 0), ("small", 0), ("txvar", 3), ("halfspace_64x64x48", 0)]
     dirs = [(case_dir(n), itx) for n, itx in cases]
     with Batch(precision=precision) as b:
         slots = [b.add(d, itx) for d, itx in dirs]
@@ -93,7 +93,7 @@ def test_batch_with_the_padded_plane(built, case_dir):
     traces in the batch as alone."""
     from tcsem_fdtd_gb300 import Batch, Simulation
 
-    dirs = [case_dir("small"), case_dir("cfg1")]
+    dirs = [case_dir("small"), case_dir("halfspace_64x64x48")]
     with Batch(precision=32, padded_plane=2) as b:
         slots = [b.add(d) for d in dirs]
         run_to_end(b)
@@ -109,7 +109,7 @@ def test_batch_layout_autotuner(built, case_dir):
     layout the slot reports."""
     from tcsem_fdtd_gb300 import Batch
 
-    dirs = [case_dir("small"), case_dir("tiny"), case_dir("cfg1")]
+    dirs = [case_dir("small"), case_dir("tiny"), case_dir("halfspace_64x64x48")]
     with Batch(precision=32, zchunks=-1) as b:
         slots = [b.add(d) for d in dirs]
         run_to_end(b)

@@ -48,7 +48,7 @@ def randomize(sim, orc, seed, names=("Ex", "Ey", "Ez", "Bx", "By", "Bz", "BxAir"
         sim.set(n, a)
 
 
-@pytest.mark.parametrize("name", ["tiny", "small", "txvar", "cfg1"])
+@pytest.mark.parametrize("name", ["tiny", "small", "txvar", "halfspace_64x64x48"])
 def test_setup_and_schedule_match_oracle(built, case_dir, name):
     sim, orc = pair(case_dir, name, 64)
     i = sim.info
@@ -92,7 +92,7 @@ def test_bderivate_stage(built, case_dir, name, precision):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-@pytest.mark.parametrize("name", ["tiny", "small", "cfg1", "cfg2", "cfg3"])  # planes up to 832 x 180 and 736 x 736
+@pytest.mark.parametrize("name", ["tiny", "small", "halfspace_64x64x48", "marine1d_128x128x96", "marine3d_256x256x160"])  # planes up to 832 x 180 and 736 x 736
 def test_upcontinuation_stage(built, case_dir, name, precision):
     sim, orc = pair(case_dir, name, precision)
     randomize(sim, orc, 11, names=("Bz",))
@@ -181,7 +181,7 @@ def test_full_run_fp32_within_one_percent(built, case_dir, name):
 # factor above 5): 96 x 80, 450 x 270, 864 x 180
 @pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("precision", [64, 32])
-@pytest.mark.parametrize("name", ["small", "cfg1", "cfg2"])
+@pytest.mark.parametrize("name", ["small", "halfspace_64x64x48", "marine1d_128x128x96"])
 def test_padded_upcontinuation_stage(built, case_dir, name, precision, mode):
     """The padded-plane options against the oracle's padded continuation."""
     sim, orc = pair(case_dir, name, precision, padded_plane=mode)
@@ -211,7 +211,7 @@ def test_fp32_against_fp64_on_the_marine_survey(built, case_dir):
     ratio.  Measured 1.3e-4."""
     from tcsem_fdtd_gb300 import Simulation
 
-    d = case_dir("cfg2")
+    d = case_dir("marine1d_128x128x96")
     tr = {}
     for p in (64, 32):
         with Simulation(d, precision=p) as sim:

@@ -34,7 +34,7 @@ def alone(d, itx=0):
 def stream(case_dir):
     from tcsem_fdtd_gb300.serve import Request
 
-    names = [("small", 0), ("tiny", 0), ("txvar", 2), ("cfg1", 0), ("tiny", 0), ("txvar", 4)]
+    names = [("small", 0), ("tiny", 0), ("txvar", 2), ("halfspace_64x64x48", 0), ("tiny", 0), ("txvar", 4)]
     return [Request(r, case_dir(n), 0.02 * r, itx) for r, (n, itx) in enumerate(names)]
 
 

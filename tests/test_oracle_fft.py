@@ -22,7 +22,7 @@ def test_oracle_continuation_is_linear(name, case_dir):
         np.testing.assert_allclose(outs[2][q], lin, rtol=0, atol=1e-11 * np.abs(lin).max())
 
 
-@pytest.mark.parametrize("name", ["tiny", "small", "cfg1"])
+@pytest.mark.parametrize("name", ["tiny", "small", "halfspace_64x64x48"])
 def test_oracle_spline_remap_keeps_core_and_is_exact_on_linear_data(name, case_dir):
     """The natural spline reproduces linear data in the strips (the end-derivative extrapolation too)."""
     from oracle.oracle import Oracle

@@ -12,7 +12,7 @@ import pytest
 
 from conftest import GOLDEN
 
-CASES = ["tiny", "small", "txvar", "example", "cfg1", "cfg2", "cfg3"]
+CASES = ["tiny", "small", "txvar", "example", "halfspace_64x64x48", "marine1d_128x128x96", "marine3d_256x256x160"]
 
 
 def load(name):

@@ -37,7 +37,7 @@ def boundary_twice(lib, sim, fn, bz):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-@pytest.mark.parametrize("name", ["small", "cfg1", "cfg3"])
+@pytest.mark.parametrize("name", ["small", "halfspace_64x64x48", "marine3d_256x256x160"])
 def test_noalloc_boundary_matches_allocating_entry(lib, case_dir, name, precision):
     from tcsem_fdtd_gb300 import Simulation
 
@@ -57,7 +57,7 @@ def test_noalloc_refuses_a_plane_beyond_the_static_scratch(lib, case_dir):
     """A 992 x 992 plane over 512 rows needs about 25 MB of FP64 scratch (> 16 MiB)."""
     from tcsem_fdtd_gb300 import Simulation, TcsemError
 
-    d = case_dir("cfg3", xsplit=(0, 40, 432, 40, 0), ysplit=(0, 40, 432), zsplit=(0, 4, 44),
+    d = case_dir("marine3d_256x256x160", xsplit=(0, 40, 432, 40, 0), ysplit=(0, 40, 432), zsplit=(0, 4, 44),
                  model=dict(kind="uniform", sigma=1.0))
     with Simulation(d, precision=64) as sim:
         assert (sim.info["L1"], sim.info["M1"]) == (992, 992)
