@@ -19,6 +19,7 @@
 //   4. bilinearly remaps into plane k = -1 of the Bx/By buffers.
 // All transforms are in-shared-memory mixed-radix Stockham FFTs of arbitrary
 // length written here (no cuFFT).
+#include "check.cuh"
 #include "kernels.cuh"
 #include "boundary.cuh"
 #include "fft.cuh"
@@ -220,7 +221,9 @@ __device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *
     for (int e = threadIdx.x; e < 2 * L; e += blockDim.x) {
         const int r = e >= L ? 1 : 0, i = e - r * L;
         T v = T(0);
-        if (r < nr) {  // plane 0 of Bz is chunk-partial: add the totals of the chunks below
+        if (r < nr && TCSEM_IN(plane + (long long)(j0 + r + 1) * g.XP + 4 + i, g.total(), bd.err) &&
+            TCSEM_IN((long long)(nch - 1) * plane + (j0 + r + 1) * g.XP + 4 + i, (long long)nch * plane, bd.err)) {
+            // plane 0 of Bz is chunk-partial: add the totals of the chunks below
             const long long o = (long long)(j0 + r + 1) * g.XP + 4 + i;
             T p[kMaxChunks];
 #pragma unroll
@@ -262,6 +265,7 @@ __device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *
     pdl_allow_next();
     for (int kx = threadIdx.x; kx < bd.H; kx += blockDim.x) {
         const C2<T> zk = Z[kx], zm = Z[kx == 0 ? 0 : L1 - kx];
+        if (!TCSEM_IN((long long)kx * bd.Mp + j0 + nr - 1, (long long)bd.H * bd.Mp, bd.err)) continue;
         C2<T> *dst = bd.FT + (size_t)kx * bd.Mp + j0;
         dst[0] = {T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
         if (nr == 2) dst[1] = {T(0.5) * (zk.y + zm.y), T(0.5) * (zm.x - zk.x)};
@@ -290,16 +294,18 @@ __device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
         const unsigned btw = (unsigned)rnd16(M1 * sizeof(C2<T>)), bt = (unsigned)rnd16(R.nT * sizeof(T)),
                        bi = (unsigned)rnd16(R.nI * sizeof(int)), bc = (unsigned)rnd16(M * sizeof(C2<T>)),
                        bg = (unsigned)rnd16(M1 * sizeof(T));
+        // a refused copy (bounds-checked builds) is left out of the expected bytes
+        const bool okc = TCSEM_IN((long long)kx * bd.Mp + bc / sizeof(C2<T>) - 1, (long long)bd.H * bd.Mp, bd.err);
         mbar_init(bar, 1);
         mbar_init_fence();
-        mbar_expect_tx(bar, btw + bt + bi + bc + 2 * bg);
+        mbar_expect_tx(bar, btw + bt + bi + (okc ? bc : 0u) + 2 * bg);
         bulk_load(tw, bd.twy, btw, bar);
         bulk_load(tab, R.tabT, bt, bar);
         bulk_load(tabi, R.tabI, bi, bar);
         bulk_load(gx, bd.Gx + (size_t)kx * bd.M1p, bg, bar);
         bulk_load(gy, bd.Gy + (size_t)kx * bd.M1p, bg, bar);
         pdl_wait_prev();  // FT is the previous kernel's output
-        bulk_load(col, bd.FT + (size_t)kx * bd.Mp, bc, bar);
+        if (okc) bulk_load(col, bd.FT + (size_t)kx * bd.Mp, bc, bar);
     }
     __syncthreads();
     if (!staged(bar, bd.err)) return;
@@ -342,6 +348,7 @@ __device__ __forceinline__ void cols_cta(const BoundaryDev<T> &bd, int blk) {
     pdl_allow_next();
     for (int s = threadIdx.x; s < bd.S; s += blockDim.x) {
         const int rr = bd.rows[s];
+        if (!TCSEM_IN((long long)s * bd.Hp + kx, (long long)bd.S * bd.Hp, bd.err)) continue;
         bd.VX[(size_t)s * bd.Hp + kx] = out[rr];
         bd.VY[(size_t)s * bd.Hp + kx] = out[M1 + rr];
     }
@@ -361,13 +368,17 @@ __device__ __forceinline__ void rows_inv_cta(const BoundaryDev<T> &bd, int blk) 
     C2<T> *b = reinterpret_cast<C2<T> *>(smem_raw + ly.b);
     if (threadIdx.x == 0) {
         const unsigned btw = (unsigned)rnd16(L1 * sizeof(C2<T>)), bv = (unsigned)rnd16(H * sizeof(C2<T>));
+        // a refused pair of copies (bounds-checked builds) is left out of the expected bytes
+        const bool okv = TCSEM_IN((long long)s * bd.Hp + bv / sizeof(C2<T>) - 1, (long long)bd.S * bd.Hp, bd.err);
         mbar_init(bar, 1);
         mbar_init_fence();
-        mbar_expect_tx(bar, btw + 2 * bv);
+        mbar_expect_tx(bar, btw + (okv ? 2 * bv : 0u));
         bulk_load(tw, bd.twx, btw, bar);
         pdl_wait_prev();  // VX and VY are the previous kernel's output
-        bulk_load(vx, bd.VX + (size_t)s * bd.Hp, bv, bar);
-        bulk_load(vy, bd.VY + (size_t)s * bd.Hp, bv, bar);
+        if (okv) {
+            bulk_load(vx, bd.VX + (size_t)s * bd.Hp, bv, bar);
+            bulk_load(vy, bd.VY + (size_t)s * bd.Hp, bv, bar);
+        }
     }
     __syncthreads();
     if (!staged(bar, bd.err)) return;
@@ -384,7 +395,8 @@ __device__ __forceinline__ void rows_inv_cta(const BoundaryDev<T> &bd, int blk) 
     const C2<T> *res = fft::run<true, 1>(a, b, bd.px, tw);
     pdl_allow_next();
     C2<T> *dst = bd.Z + (size_t)s * bd.Lu;
-    for (int x = threadIdx.x; x < bd.Lu; x += blockDim.x) dst[x] = res[bd.DL + x];
+    for (int x = threadIdx.x; x < bd.Lu; x += blockDim.x)
+        if (TCSEM_IN((long long)s * bd.Lu + x, (long long)bd.S * bd.Lu, bd.err)) dst[x] = res[bd.DL + x];
 }
 
 // ---- stage 4: bilinear remap (Blinear_BxR2IR / Blinear_ByR2IR, UpContinuation_gpu.cu:42-110)
@@ -398,6 +410,10 @@ __device__ __forceinline__ void bilinear_cta(const BoundaryDev<T> &bd, T *bx, T 
         if (e < nbx) {
             const int j = e / (L + 1), i = e % (L + 1);
             const int II = bd.bxc_II[i];
+            if (!TCSEM_IN((long long)bd.bxr_a[j] * bd.Lu + II - 1, (long long)bd.S * bd.Lu, bd.err) ||
+                !TCSEM_IN((long long)bd.bxr_b[j] * bd.Lu + II, (long long)bd.S * bd.Lu, bd.err) ||
+                !TCSEM_IN(g.at(i, j, -1), g.total(), bd.err))
+                continue;
             const T lx = bd.bxc_l[i];
             const C2<T> *ra = bd.Z + (size_t)bd.bxr_a[j] * bd.Lu, *rb = bd.Z + (size_t)bd.bxr_b[j] * bd.Lu;
             T a0 = (T(1) - lx) * ra[II - 1].x + lx * ra[II].x;
@@ -407,6 +423,10 @@ __device__ __forceinline__ void bilinear_cta(const BoundaryDev<T> &bd, T *bx, T 
         } else {
             const int e2 = e - nbx, j = e2 / L, i = e2 % L;
             const int II = bd.byc_II[i];
+            if (!TCSEM_IN((long long)bd.byr_a[j] * bd.Lu + II - 1, (long long)bd.S * bd.Lu, bd.err) ||
+                !TCSEM_IN((long long)bd.byr_b[j] * bd.Lu + II, (long long)bd.S * bd.Lu, bd.err) ||
+                !TCSEM_IN(g.at(i, j, -1), g.total(), bd.err))
+                continue;
             const T lx = bd.byc_l[i];
             const C2<T> *ra = bd.Z + (size_t)bd.byr_a[j] * bd.Lu, *rb = bd.Z + (size_t)bd.byr_b[j] * bd.Lu;
             T a0 = (T(1) - lx) * ra[II - 1].y + lx * ra[II].y;

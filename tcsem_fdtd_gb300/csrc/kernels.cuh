@@ -96,9 +96,9 @@ struct ZChunks {
 // volume.cu
 template <typename T>
 void launch_update_e(const Geom &g, FieldSet<T> f, const T *con, const Axis<T> &ax, StepScalars<T> s,
-                     const SourceTable<T> &src, cudaStream_t st);
+                     const SourceTable<T> &src, int *err, cudaStream_t st);
 template <typename T>
-void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, cudaStream_t st);
+void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, int *err, cudaStream_t st);
 // TMA descriptors of the fused sweep's inputs: ex ey ez bx by bz of one field set, then sigma
 struct SweepMaps {
     CUtensorMap m[7];

@@ -8,6 +8,7 @@
 // produced in a step uses slot 0 (written in an earlier step) and the slot-1
 // value being computed, so the time interpolation is fused into the spatial
 // pass and needs no grid-wide synchronisation.
+#include "check.cuh"
 #include "kernels.cuh"
 #include "rx.cuh"
 
@@ -33,11 +34,14 @@ __device__ __forceinline__ T stencil_value(const RxDev<T> &rd, const FieldSet<T>
             while (cz + 1 < zc.n && k3 + c >= zc.kb[cz + 1]) cz++;
 #pragma unroll
         for (int b = 0; b < 4; b++) {
-            const T *row = F + base + (long long)c * g.PS + (long long)b * g.XP;
+            const long long o = base + (long long)c * g.PS + (long long)b * g.XP;
+            if (!TCSEM_IN(o, g.total(), rd.err) || !TCSEM_IN(o + 3, g.total(), rd.err)) continue;
+            const T *row = F + o;
             T r0 = row[0], r1 = row[1], r2 = row[2], r3 = row[3];
             if (comp == 5 && zc.n > 1) {
                 const long long cb = col + (long long)b * g.XP;
                 for (int q = cz + 1; q < zc.n; q++) {
+                    if (!TCSEM_IN(q * plane + cb + 3, zc.n * plane, rd.err)) continue;
                     const T *t = tot + q * plane + cb;
                     r0 += t[0]; r1 += t[1]; r2 += t[2]; r3 += t[3];
                 }
@@ -60,13 +64,15 @@ __device__ __forceinline__ void rx_thread(const RxDev<T> &rd, const FieldSet<T> 
     const int slot = efield ? act.e_slot : act.b_slot;
     if (slot < 0) return;
     const T v = stencil_value(rd, f, idx, g, tot, zc);
+    if (!TCSEM_IN((long long)slot * NC * nr + idx, 2LL * NC * nr, rd.err)) return;
     rd.ef0[(size_t)slot * NC * nr + idx] = v;
     const int first = efield ? act.e_first : act.b_first, count = efield ? act.e_count : act.b_count;
     const T *l1 = efield ? rd.e_l1 : rd.b_l1;
     if (slot == 1) {  // EFTimeInterp / BFTimeInterp, EFInterp2Rx.cu:380-407
         const T v0 = rd.ef0[idx];
         for (int s = first; s < first + count; s++)
-            rd.efs[((size_t)r * NC + p) * rd.Nt + s] = (T(1) - l1[s]) * v0 + l1[s] * v;
+            if (TCSEM_IN(((long long)r * NC + p) * rd.Nt + s, (long long)nr * NC * rd.Nt, rd.err))
+                rd.efs[((size_t)r * NC + p) * rd.Nt + s] = (T(1) - l1[s]) * v0 + l1[s] * v;
     }
 }
 

@@ -22,6 +22,7 @@ template <typename T> struct RxDev {
     T *efs;                     // [nr][NComp][Nt]
     const T *e_l1, *b_l1;       // per sample: time-interpolation weight
     const StepEntryActs *acts;  // per step
+    int *err;                   // device error word (bounds-checked builds)
 };
 
 template <typename T>

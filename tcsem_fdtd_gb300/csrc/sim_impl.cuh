@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "boundary.cuh"
+#include "check.cuh"
 #include "kernels.cuh"
 #include "rx.cuh"
 #include "setup.h"
@@ -443,6 +444,8 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaMemcpy(&h, errw.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (h) {
             CK(cudaMemset(errw.p, 0, sizeof(int)));
+            if (h == TCSEM_CHECK_CODE)
+                throw Error(TCSEM_ERR_CUDA, "a kernel index fell outside its array (bounds-checked build)");
             throw Error(TCSEM_ERR_CUDA, "a bounded wait in a kernel gave up (a bulk copy did not arrive)");
         }
     }
@@ -694,6 +697,7 @@ template <typename T> struct SimImpl : SimBase {
         rd.base = rx_base.as<long long>(); rd.comp = rx_comp.as<int>(); rd.w = rx_w.as<T>();
         rd.ef0 = ef0.as<T>(); rd.efs = efs.as<T>(); rd.e_l1 = e_l1.as<T>(); rd.b_l1 = b_l1.as<T>();
         rd.acts = acts.as<StepEntryActs>();
+        rd.err = errw.as<int>();
         itx = t;
         for (auto &e : gexec) if (e) { cudaGraphExecDestroy(e); e = nullptr; }
     }
@@ -867,12 +871,12 @@ template <typename T> struct SimImpl : SimBase {
     void electric_field(double lam, double dt, double wave) override {
         need_tx();
         consolidate(cur);
-        launch_update_e<T>(g, fs(cur), con.as<T>(), ax, scal(lam, dt, 0, wave), src, stream);
+        launch_update_e<T>(g, fs(cur), con.as<T>(), ax, scal(lam, dt, 0, wave), src, errw.as<int>(), stream);
         CK(cudaGetLastError());
     }
     void bderivate(double dtb) override {
         consolidate(cur);
-        launch_bderivate<T>(g, fs(cur), ax, (T)dtb, stream);
+        launch_bderivate<T>(g, fs(cur), ax, (T)dtb, errw.as<int>(), stream);
         CK(cudaGetLastError());
     }
     void fused_step(double lam, double dt, double dtb, double wave) override {

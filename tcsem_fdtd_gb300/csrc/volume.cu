@@ -13,6 +13,7 @@
 //    its neighbours.  Algorithmic traffic: 7 words read + 6 written per cell.
 #include "kernels.cuh"
 #include "async.cuh"
+#include "check.cuh"
 
 namespace tcsem {
 
@@ -34,7 +35,7 @@ __device__ __forceinline__ T df_update(const StepScalars<T> &s, T sigma, T e_old
 // ----------------------------------------------------- reference-structured
 
 template <typename T>
-__global__ void k_update_e(Geom g, FieldSet<T> f, const T *__restrict__ con, Axis<T> ax, StepScalars<T> s) {
+__global__ void k_update_e(Geom g, FieldSet<T> f, const T *__restrict__ con, Axis<T> ax, StepScalars<T> s, int *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.L || j >= g.M) return;
     const long long PS = g.PS, XP = g.XP;
@@ -42,6 +43,7 @@ __global__ void k_update_e(Geom g, FieldSet<T> f, const T *__restrict__ con, Axi
     const T rdy2 = vx ? ax.rdy2[j] : T(0), rdx2 = vy ? ax.rdx2[i] : T(0);
     long long c = g.at(i, j, 0);
     for (int k = 0; k < g.N; k++, c += PS) {
+        if (!TCSEM_IN(c + PS, g.total(), err) || !TCSEM_IN(c - PS - XP - 1, g.total(), err)) continue;
         const T rzs = ax.rdzs[k];
         if (vx) {  // UpdateEx, ElectricalFiled.cu:89-175
             T sg = T(0.5) * (T(0.5) * (con[c - XP] + con[c]) + T(0.5) * (con[c - PS - XP] + con[c - PS]));
@@ -63,13 +65,13 @@ __global__ void k_update_e(Geom g, FieldSet<T> f, const T *__restrict__ con, Axi
 
 // AddTx_x/_y/_z (ElectricalFiled.cu:347-475): one thread per injected cell
 template <typename T>
-__global__ void k_source(Geom g, FieldSet<T> f, SourceTable<T> src, T wave) {
+__global__ void k_source(Geom g, FieldSet<T> f, SourceTable<T> src, T wave, int *err) {
     for (int sgi = 0; sgi < src.nseg; sgi++) {
         for (int q = threadIdx.x; q < src.count[sgi]; q += blockDim.x) {
             int i = src.i[sgi], j = src.j[sgi], k = src.k[sgi];
             T *e = src.comp[sgi] == 0 ? f.ex : src.comp[sgi] == 1 ? f.ey : f.ez;
             if (src.comp[sgi] == 0) i += q; else if (src.comp[sgi] == 1) j += q; else k += q;
-            e[g.at(i, j, k)] -= wave * src.coef[src.off[sgi] + q];
+            if (TCSEM_IN(g.at(i, j, k), g.total(), err)) e[g.at(i, j, k)] -= wave * src.coef[src.off[sgi] + q];
         }
         __syncthreads();
     }
@@ -77,13 +79,14 @@ __global__ void k_source(Geom g, FieldSet<T> f, SourceTable<T> src, T wave) {
 
 // UpdateBx/UpdateBy, Bderivate.cu:79-200
 template <typename T>
-__global__ void k_update_bxy(Geom g, FieldSet<T> f, Axis<T> ax, T dtb) {
+__global__ void k_update_bxy(Geom g, FieldSet<T> f, Axis<T> ax, T dtb, int *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.L || j >= g.M) return;
     const long long PS = g.PS, XP = g.XP;
     const T rdy = ax.rdy[j], rdx = ax.rdx[i];
     long long c = g.at(i, j, 0);
     for (int k = 0; k < g.N; k++, c += PS) {
+        if (!TCSEM_IN(c + PS, g.total(), err) || !TCSEM_IN(c, g.total(), err)) continue;
         const T rdz = ax.rdz[k];
         if (i >= 1) f.bx[c] += ((f.ey[c + PS] - f.ey[c]) * rdz - (f.ez[c + XP] - f.ez[c]) * rdy) * dtb;
         if (j >= 1) f.by[c] += ((f.ez[c + 1] - f.ez[c]) * rdx - (f.ex[c + PS] - f.ex[c]) * rdz) * dtb;
@@ -92,7 +95,7 @@ __global__ void k_update_bxy(Geom g, FieldSet<T> f, Axis<T> ax, T dtb) {
 
 // UpdateBz, Bderivate.cu:202-265: div B = 0, integrated from the bottom up
 template <typename T>
-__global__ void k_update_bz(Geom g, FieldSet<T> f, Axis<T> ax) {
+__global__ void k_update_bz(Geom g, FieldSet<T> f, Axis<T> ax, int *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.L || j >= g.M) return;
     const long long PS = g.PS, XP = g.XP;
@@ -100,6 +103,7 @@ __global__ void k_update_bz(Geom g, FieldSet<T> f, Axis<T> ax) {
     long long c = g.at(i, j, g.N - 1);
     T acc = T(0);
     for (int k = g.N - 1; k >= 0; k--, c -= PS) {
+        if (!TCSEM_IN(c + XP, g.total(), err) || !TCSEM_IN(c, g.total(), err)) continue;
         acc += ax.dzk[k] * ((f.bx[c + 1] - f.bx[c]) * rdx + (f.by[c + XP] - f.by[c]) * rdy);
         f.bz[c] = acc;
     }
@@ -107,17 +111,17 @@ __global__ void k_update_bz(Geom g, FieldSet<T> f, Axis<T> ax) {
 
 template <typename T>
 void launch_update_e(const Geom &g, FieldSet<T> f, const T *con, const Axis<T> &ax, StepScalars<T> s,
-                     const SourceTable<T> &src, cudaStream_t st) {
+                     const SourceTable<T> &src, int *err, cudaStream_t st) {
     dim3 blk(32, 8), grd((g.L + 31) / 32, (g.M + 7) / 8);
-    k_update_e<T><<<grd, blk, 0, st>>>(g, f, con, ax, s);
-    if (src.nseg > 0 && s.wave != T(0)) k_source<T><<<1, 128, 0, st>>>(g, f, src, s.wave);
+    k_update_e<T><<<grd, blk, 0, st>>>(g, f, con, ax, s, err);
+    if (src.nseg > 0 && s.wave != T(0)) k_source<T><<<1, 128, 0, st>>>(g, f, src, s.wave, err);
 }
 
 template <typename T>
-void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, cudaStream_t st) {
+void launch_bderivate(const Geom &g, FieldSet<T> f, const Axis<T> &ax, T dtb, int *err, cudaStream_t st) {
     dim3 blk(32, 8), grd((g.L + 31) / 32, (g.M + 7) / 8);
-    k_update_bxy<T><<<grd, blk, 0, st>>>(g, f, ax, dtb);
-    k_update_bz<T><<<grd, blk, 0, st>>>(g, f, ax);
+    k_update_bxy<T><<<grd, blk, 0, st>>>(g, f, ax, dtb, err);
+    k_update_bz<T><<<grd, blk, 0, st>>>(g, f, ax, err);
 }
 
 // ------------------------------------------------------------- fused sweep
@@ -180,6 +184,8 @@ template <typename T> struct SweepThread {
     const CUtensorMap *maps;
     unsigned plane_bytes;
     int j, PS, N, k0, k1, klow, ktop, tid, i0, j0;
+    int total;  // elements of each field array (bounds-checked builds)
+    int *err;
     T rdy2, rdy, fy;  // per row: 1/(dy[j-1]+dy[j]), 1/dy[j], dtb/dy[j]
     // per cell
     int so[fs3::NC], xo[fs3::NC], i[fs3::NC], col[fs3::NC];
@@ -212,7 +218,7 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
             const T by = t.byo1[c] + (ezi - t.ezn[c]) * t.fx[c] - (t.ex1[c] - t.exn[c]) * fz;
             t.bxn[c] = t.vEy[c] ? bx : t.bxo1[c];
             t.byn[c] = t.vEx[c] ? by : t.byo1[c];
-            if (t.own[c]) {
+            if (t.own[c] && TCSEM_IN(t.col[c] + (k + 2) * t.PS, t.total, t.err)) {
                 const int o = t.col[c] + (k + 2) * t.PS;
                 out.bx[o] = t.bxn[c];
                 out.by[o] = t.byn[c];
@@ -284,7 +290,7 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
         }
 #pragma unroll
         for (int c = 0; c < NC; c++) {
-            if (upd && lo && t.own[c]) {
+            if (upd && lo && t.own[c] && TCSEM_IN(t.col[c] + (k + 1) * t.PS, t.total, t.err)) {
                 const int o = t.col[c] + (k + 1) * t.PS;
                 out.ex[o] = t.exn[c];
                 out.ey[o] = t.eyn[c];
@@ -325,7 +331,7 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
         for (int c = 0; c < NC; c++) {
             t.acc[c] += dz * ((t.x_bxn[QB * XP2 + t.xo[c] + 1] - t.bxn[c]) * t.rdx[c] +
                               (t.x_byn[QB * XP2 + t.xo[c] + XC] - t.byn[c]) * t.rdy);
-            if (t.own[c]) out.bz[t.col[c] + (k + 2) * t.PS] = t.acc[c];
+            if (t.own[c] && TCSEM_IN(t.col[c] + (k + 2) * t.PS, t.total, t.err)) out.bz[t.col[c] + (k + 2) * t.PS] = t.acc[c];
         }
     }
     return true;
@@ -359,6 +365,8 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
     const int L = g.L, M = g.M, N = g.N, XP = g.XP;
     t.N = N;
     t.PS = (int)g.PS;
+    t.total = (int)g.total();
+    t.err = err;
     t.k0 = zc.plane(c);
     t.k1 = zc.plane(c + 1);
     const int ty = w < 9 ? w : lane;
@@ -418,7 +426,8 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
                 const int pc = gy * XP + gx;
                 T pv[kMaxChunks];  // all loads in flight together
 #pragma unroll
-                for (int q = 1; q < kMaxChunks; q++) pv[q] = q > c && q < zc.n ? ldg(tin + q * t.PS + pc) : T(0);
+                for (int q = 1; q < kMaxChunks; q++)
+                    pv[q] = q > c && q < zc.n && TCSEM_IN(q * t.PS + pc, zc.n * t.PS, err) ? ldg(tin + q * t.PS + pc) : T(0);
                 const T first = c + 1 < zc.n ? ldg(tin + (c + 1) * t.PS + pc) : T(0);
 #pragma unroll
                 for (int q = 1; q < kMaxChunks; q++)
@@ -483,7 +492,7 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
     if (zc.n > 1) {
 #pragma unroll
         for (int q = 0; q < NC; q++)
-            if (t.own[q]) tout[c * t.PS + t.col[q]] = t.acc[q];
+            if (t.own[q] && TCSEM_IN(c * t.PS + t.col[q], zc.n * t.PS, err)) tout[c * t.PS + t.col[q]] = t.acc[q];
     }
 }
 
@@ -572,8 +581,8 @@ template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, c
 
 #define INST(T)                                                                                                    \
     template void launch_update_e<T>(const Geom &, FieldSet<T>, const T *, const Axis<T> &, StepScalars<T>,        \
-                                     const SourceTable<T> &, cudaStream_t);                                        \
-    template void launch_bderivate<T>(const Geom &, FieldSet<T>, const Axis<T> &, T, cudaStream_t);                \
+                                     const SourceTable<T> &, int *, cudaStream_t);                                 \
+    template void launch_bderivate<T>(const Geom &, FieldSet<T>, const Axis<T> &, T, int *, cudaStream_t);         \
     template void launch_fused_sweep<T>(const SweepMaps &, const Geom &, FieldSet<T>, const T *, T *,             \
                                         const Axis<T> &, StepScalars<T>, const StepScalars<T> *, StepGate,         \
                                         const SourceTable<T> &, const ZChunks &, int, int, bool, int *, cudaStream_t);       \
