@@ -48,10 +48,14 @@ class Request:
 class Server:
     """Continuous batching of survey requests on one GPU."""
 
-    def __init__(self, precision=32, device=0, budget=64 << 30, block=64, zchunks=0):
-        from .api import Batch
+    def __init__(self, precision=32, device=0, budget=64 << 30, block=64, zchunks=0, batch=None):
+        """`batch`: an object with the methods of :class:`~tcsem_fdtd_gb300.api.Batch` used here
+        (add, advance, poll, info, traces, remove, close); a device batch by default."""
+        if batch is None:
+            from .api import Batch
 
-        self.batch = Batch(precision=precision, device=device, budget=budget, graph_steps=block, zchunks=zchunks)
+            batch = Batch(precision=precision, device=device, budget=budget, graph_steps=block, zchunks=zchunks)
+        self.batch = batch
         self.block = block
         self.queue, self.running, self.done = [], {}, []
 
