@@ -99,6 +99,17 @@ tcsem_status tcsem_advance(tcsem_sim_t *sim, long nsteps, int *done);
 tcsem_status tcsem_get_traces(tcsem_sim_t *sim, double *traces);
 tcsem_status tcsem_synchronize(tcsem_sim_t *sim);
 
+/* Checkpoint of a run in progress (no counterpart in the reference; for moving
+ * or preempting long runs): save_state writes, after tcsem_begin and any number
+ * of tcsem_advance calls, what the next step needs -- the current fields, their
+ * Bz chunk totals, the receiver samples so far and the step -- to `path`;
+ * load_state reads it into a handle opened on the same survey with the same
+ * precision and z-chunk layout (TCSEM_ERR_INVALID otherwise), after which
+ * tcsem_advance continues the run: its traces equal those of the uninterrupted
+ * run bit for bit. */
+tcsem_status tcsem_save_state(tcsem_sim_t *sim, const char *path);
+tcsem_status tcsem_load_state(tcsem_sim_t *sim, const char *path);
+
 /* Per-stage entry points, the seam of FTDT.h:291-344.  They act on the
  * handle's current fields like the reference's functions act on DArrays:
  *   tcsem_upcontinuation   <- UpContinuation_gpu (UpContinuation_gpu.cu:166)

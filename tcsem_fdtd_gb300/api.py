@@ -71,6 +71,8 @@ def library():
         "tcsem_advance": (i, [vp, l_, ip]),
         "tcsem_get_traces": (i, [vp, dp]),
         "tcsem_synchronize": (i, [vp]),
+        "tcsem_save_state": (i, [vp, C.c_char_p]),
+        "tcsem_load_state": (i, [vp, C.c_char_p]),
         "tcsem_select_tx": (i, [vp, i]),
         "tcsem_upcontinuation": (i, [vp]),
         "tcsem_upcontinuation_noalloc": (i, [vp]),
@@ -195,6 +197,14 @@ class Simulation:
 
     def synchronize(self):
         self._check(library().tcsem_synchronize(self._h))
+
+    def save_state(self, path):
+        """tcsem_save_state: checkpoint of the run in progress."""
+        self._check(library().tcsem_save_state(self._h, os.fsencode(path)))
+
+    def load_state(self, path):
+        """tcsem_load_state: continue a saved run (same survey, precision and z-chunk layout)."""
+        self._check(library().tcsem_load_state(self._h, os.fsencode(path)))
 
     # -------------------------------------------------------------- stage seam
     def select_tx(self, itx):

@@ -140,6 +140,18 @@ tcsem_status tcsem_get_traces(tcsem_sim_t *s, double *t) {
         b.traces(t);
     });
 }
+tcsem_status tcsem_save_state(tcsem_sim_t *s, const char *path) {
+    return guard(s, [&](SimBase &b) {
+        if (!path) throw Error(TCSEM_ERR_INVALID, "null path");
+        b.save_state(path);
+    });
+}
+tcsem_status tcsem_load_state(tcsem_sim_t *s, const char *path) {
+    return guard(s, [&](SimBase &b) {
+        if (!path) throw Error(TCSEM_ERR_INVALID, "null path");
+        b.load_state(path);
+    });
+}
 tcsem_status tcsem_synchronize(tcsem_sim_t *s) {
     return guard(s, [&](SimBase &b) {
         CK(cudaStreamSynchronize(b.stream));

@@ -132,6 +132,8 @@ struct SimBase {
     virtual void time_steps(int itx, long n, double *tot, double *sweep, double *bnd) = 0;
     virtual void timed_advance(long n, double *ms) = 0;
     virtual void check_error() = 0;
+    virtual void save_state(const char *path) = 0;
+    virtual void load_state(const char *path) = 0;
     size_t field_count(int comp) const {
         size_t L = model.L, M = model.M, N = model.N;
         switch (comp) {
@@ -941,6 +943,100 @@ template <typename T> struct SimImpl : SimBase {
         }
         if (comp == TCSEM_BZ)  // a plain Bz plane: no chunk offsets
             for (int b = 0; b < 2; b++) CK(cudaMemset(tot[b].p, 0, tot[b].n));
+    }
+
+    // ---- checkpoint of a run in progress: what one step hands the next (the field set the
+    // next step reads, its Bz chunk totals, the receiver slots and traces so far, the step)
+    struct StateHeader {
+        char magic[8];
+        int version, tsize, L, M, N, itx, cur, nch;
+        int kb[kMaxChunks + 1];
+        long long step, field_bytes, tot_bytes, ef0_bytes, efs_bytes;
+    };
+    void save_state(const char *path) override {
+        if (!begun) throw Error(TCSEM_ERR_STATE, "tcsem_begin must precede tcsem_save_state");
+        CK(cudaStreamSynchronize(stream));
+        check_device_error();
+        StateHeader h{};
+        std::memcpy(h.magic, "TCSEMST", 8);
+        h.version = 1; h.tsize = (int)sizeof(T); h.L = model.L; h.M = model.M; h.N = model.N;
+        h.itx = itx; h.cur = cur; h.nch = zc.n;
+        for (int c = 0; c <= kMaxChunks; c++) h.kb[c] = zc.kb[c];
+        h.step = step;
+        h.field_bytes = (long long)fld[cur][0].n;
+        h.tot_bytes = (long long)zc.n * g.PS * (long long)sizeof(T);
+        h.ef0_bytes = (long long)ef0.n;
+        h.efs_bytes = (long long)efs.n;
+        std::FILE *f = std::fopen(path, "wb");
+        if (!f) throw Error(TCSEM_ERR_IO, std::string("cannot write ") + path);
+        std::vector<unsigned char> buf;
+        bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+        auto put = [&](const void *dev, size_t n) {
+            buf.resize(n);
+            if (n) CK(cudaMemcpy(buf.data(), dev, n, cudaMemcpyDeviceToHost));
+            ok = ok && std::fwrite(buf.data(), 1, n, f) == n;
+        };
+        try {
+            for (int c = 0; c < 6; c++) put(fld[cur][c].p, (size_t)h.field_bytes);
+            put(tot[cur].p, (size_t)h.tot_bytes);
+            put(ef0.p, (size_t)h.ef0_bytes);
+            put(efs.p, (size_t)h.efs_bytes);
+        } catch (...) {
+            std::fclose(f);
+            throw;
+        }
+        ok = (std::fclose(f) == 0) && ok;
+        if (!ok) throw Error(TCSEM_ERR_IO, std::string("cannot write ") + path);
+    }
+    // into a handle of the same survey, precision and z-chunk layout; the run continues with advance
+    void load_state(const char *path) override {
+        std::FILE *f = std::fopen(path, "rb");
+        if (!f) throw Error(TCSEM_ERR_IO, std::string("cannot open ") + path);
+        StateHeader h{};
+        std::vector<unsigned char> buf;
+        bool ok = std::fread(&h, sizeof h, 1, f) == 1;
+        auto fail = [&](tcsem_status st, const std::string &m) {
+            std::fclose(f);
+            throw Error(st, m);
+        };
+        if (!ok || std::memcmp(h.magic, "TCSEMST", 8) != 0 || h.version != 1) fail(TCSEM_ERR_PARSE, std::string(path) + " is not a saved run state");
+        bool same = h.tsize == (int)sizeof(T) && h.L == model.L && h.M == model.M && h.N == model.N && h.nch == zc.n &&
+                    h.field_bytes == (long long)fld[0][0].n && h.tot_bytes == (long long)zc.n * g.PS * (long long)sizeof(T) &&
+                    (h.cur == 0 || h.cur == 1) && h.step >= 0 && h.step <= sched.nsteps && h.itx >= 0 &&
+                    h.itx < (int)model.in.tx.size();
+        for (int c = 0; c <= zc.n && same; c++) same = h.kb[c] == zc.kb[c];
+        const std::string other = std::string(path) + " was saved by a different survey, precision or z-chunk layout";
+        if (!same) fail(TCSEM_ERR_INVALID, other);
+        try {
+            begin(h.itx);  // the transmitter's tables (receiver buffers) and a zero state, then the saved arrays
+        } catch (...) {
+            std::fclose(f);
+            throw;
+        }
+        if (h.ef0_bytes != (long long)ef0.n || h.efs_bytes != (long long)efs.n) fail(TCSEM_ERR_INVALID, other);
+        auto get = [&](void *dev, size_t n) {
+            buf.resize(n);
+            ok = ok && std::fread(buf.data(), 1, n, f) == n;
+            if (ok && n) CK(cudaMemcpy(dev, buf.data(), n, cudaMemcpyHostToDevice));
+        };
+        try {
+            for (int c = 0; c < 6; c++) get(fld[h.cur][c].p, (size_t)h.field_bytes);
+            get(tot[h.cur].p, (size_t)h.tot_bytes);
+            get(ef0.p, (size_t)h.ef0_bytes);
+            get(efs.p, (size_t)h.efs_bytes);
+        } catch (...) {
+            std::fclose(f);
+            throw;
+        }
+        std::fclose(f);
+        if (!ok) {
+            zero_state();
+            throw Error(TCSEM_ERR_IO, std::string(path) + " is truncated");
+        }
+        const int s = (int)h.step;
+        CK(cudaMemcpy(gate_base.p, &s, sizeof(int), cudaMemcpyHostToDevice));
+        cur = h.cur;
+        step = h.step;
     }
 
     void timed_advance(long n, double *ms_out) override {
