@@ -103,3 +103,32 @@ def test_cli_usage_error_exit_code():
     build.build()
     r = subprocess.run([build.CLI, "--bogus"], capture_output=True, text=True)
     assert r.returncode == 2
+
+
+def test_integration_snippets_compile_against_the_header(tmp_path):
+    """The C code INTEGRATION.md gives a maintainer compiles against include/tcsem.h and links
+    against the library's exported symbols (gcc; the snippets placed in a main())."""
+    import re
+    import shutil
+    import subprocess
+
+    from tcsem_fdtd_gb300.api import HEADER
+
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    text = open(os.path.join(os.path.dirname(HEADER), "..", "INTEGRATION.md")).read()
+    blocks = re.findall(r"```c\n(.*?)```", text, flags=re.S)
+    assert len(blocks) >= 2
+    body = "\n".join(b for b in blocks if "#include" not in b)
+    first = next(b for b in blocks if "#include" in b)
+    src = tmp_path / "snippet.c"
+    src.write_text("#include <stdio.h>\n#include <stdlib.h>\n" + first.split("\n", 1)[0] + "\n"
+                   "int main(void) {\n" + first.split("\n", 1)[1] + "\n{\n" + body + "\n}\nreturn 0;\n}\n")
+    lib_dir = os.path.dirname(__import__("tcsem_fdtd_gb300").api.LIB_PATH)
+    cmd = ["gcc", "-std=c99", "-Wall", "-Werror", "-Wno-unused-variable", "-I", os.path.dirname(HEADER), str(src)]
+    if os.path.exists(os.path.join(lib_dir, "libtcsem.so")):  # link against the exported symbols
+        cmd += ["-o", str(tmp_path / "snippet"), "-L", lib_dir, "-ltcsem"]
+    else:  # compile only
+        cmd += ["-c", "-o", str(tmp_path / "snippet.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
