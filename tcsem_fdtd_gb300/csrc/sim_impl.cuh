@@ -453,8 +453,15 @@ template <typename T> struct SimImpl : SimBase {
     }
     void sweep(int b, StepScalars<T> s, const StepScalars<T> *table, StepGate gate, int c0 = 0, int c1 = -1,
                cudaStream_t st = nullptr) {
+        if (c1 < 0) c1 = zc.n;
+        // Block order: consecutive steps alternate the chunk order (a step starts on the planes
+        // the previous one wrote last), except in a launch that includes a top chunk shorter than
+        // the others -- its blocks go last, so its short CTAs take the slots the single wave of
+        // the others leaves free instead of delaying them (measured: 119.0 µs for the whole
+        // 256 x 256 x 160 sweep against 121.8 alternating and 125.4 with the top chunk first)
+        const bool short_top = c0 == 0 && c1 - c0 > 1 && zc.kb[1] - zc.kb[0] < zc.kb[2] - zc.kb[1];
         launch_fused_sweep<T>(maps[b], g, fs(b ^ 1), tot[b].as<T>(), tot[b ^ 1].as<T>(), ax, s, table, gate, src, zc,
-                              c0, c1 < 0 ? zc.n : c1, (b & 1) != 0, errw.as<int>(), st ? st : stream);
+                              c0, c1, short_top || (b & 1) != 0, errw.as<int>(), st ? st : stream);
     }
     void consolidate(int b) { launch_bz_consolidate<T>(g, fs(b).bz, tot[b].as<T>(), zc, stream); }
 
