@@ -141,6 +141,15 @@ template <typename T> struct BatchImpl : BatchBase {
         running.clear();
         for (int q = 0; q < (int)slots.size(); q++)
             if (!slots[q].finished()) running.push_back(q);
+        // the slots whose CTAs march the most planes first (longest processing time first: the
+        // sweep's last wave is then made of short CTAs; 16 generated surveys 698 -> 672 us/step)
+        auto depth = [&](int q) {
+            const ZChunks &z = slots[q].sim->zc;
+            int d = 0;
+            for (int c = 0; c < z.n; c++) d = std::max(d, z.kb[c + 1] - z.kb[c]);
+            return d;
+        };
+        std::stable_sort(running.begin(), running.end(), [&](int a, int b) { return depth(a) > depth(b); });
         const int n = (int)running.size();
         std::vector<SweepSlot<T>> hsw[2];
         std::vector<BoundarySlot<T>> hbs[2];
