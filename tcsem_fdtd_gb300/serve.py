@@ -2,7 +2,7 @@
 continuous batching, and their latencies.
 
     python -m tcsem_fdtd_gb300.serve [--requests 48] [--rate 4.0] [--seed 5]
-                                     [--budget-gb 64] [--plain]
+                                     [--budget-gb 64] [--plain] [--jsonl PATH]
 
 A :class:`Server` owns one device batch (tcsem_batch_* of include/tcsem.h).
 Each loop iteration (one graph block of the batch, `block` steps) it
@@ -116,8 +116,17 @@ def make_stream(n, rate, seed, size=((64, 256), (64, 256), (48, 160)), tn=(1.0, 
     return reqs
 
 
-def serve(reqs, server, speed=1.0):
-    """Replay the arrivals in real time (scaled by `speed`); returns the wall time of the run."""
+def request_record(req, mode="batched"):
+    """One JSON-lines record of a finished request: its times, latency and work."""
+    return {"request": req.rid, "mode": mode, "arrival_s": req.arrival, "admitted_s": req.admitted,
+            "completed_s": req.completed, "latency_s": req.completed - req.arrival,
+            "queued_s": req.admitted - req.arrival, "cell_steps": req.cells_steps,
+            "Gcell_steps_per_s": req.cells_steps / max(req.completed - req.admitted, 1e-12) / 1e9}
+
+
+def serve(reqs, server, speed=1.0, log=None):
+    """Replay the arrivals in real time (scaled by `speed`); returns the wall time of the run.
+    `log`: a text file that receives one JSON line per request as it finishes."""
     t0 = time.perf_counter()
     now = lambda: (time.perf_counter() - t0) * speed  # noqa: E731
     pending = sorted(reqs, key=lambda r: r.arrival)
@@ -129,7 +138,10 @@ def serve(reqs, server, speed=1.0):
             if pending:  # idle until the next arrival
                 time.sleep(max(0.0, (pending[0].arrival - now()) / speed))
             continue
-        server.step(now)
+        for req in server.step(now):
+            if log is not None:
+                log.write(json.dumps(request_record(req)) + "\n")
+                log.flush()
     return now()
 
 
@@ -168,16 +180,20 @@ def main(argv=None):
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--tn", type=float, nargs="+", default=[1.0, 10.0])
     ap.add_argument("--plain", action="store_true", help="also serve the stream one request at a time")
+    ap.add_argument("--jsonl", default=None, help="write one JSON line per finished request to this file")
     a = ap.parse_args(argv)
     from . import build
 
     build.build()
     reqs = make_stream(a.requests, a.rate, a.seed, tn=tuple(a.tn))
     srv = Server(budget=int(a.budget_gb * (1 << 30)), block=a.block)
+    log = open(a.jsonl, "w") if a.jsonl else None
     try:
-        out = {"batched": summary(reqs, serve(reqs, srv))}
+        out = {"batched": summary(reqs, serve(reqs, srv, log=log))}
     finally:
         srv.close()
+        if log:
+            log.close()
     if a.plain:
         plain = [Request(r.rid, r.directory, r.arrival) for r in reqs]
         out["plain"] = summary(plain, run_plain(plain))

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from tcsem_fdtd_gb300.api import TcsemError
-from tcsem_fdtd_gb300.serve import Request, Server, serve, summary
+from tcsem_fdtd_gb300.serve import Request, Server, request_record, serve, summary
 
 
 class FakeBatch:
@@ -106,3 +106,19 @@ def test_a_request_larger_than_the_whole_budget_is_reported():
     with pytest.raises(TcsemError) as e:
         srv.step(lambda: 0.0)
     assert e.value.status == 5
+
+
+def test_one_json_line_per_finished_request(tmp_path):
+    import io
+    import json
+
+    reqs, sizes, steps = stream(5, 0.001, sizes=[2], steps=[64, 128])
+    srv = Server(block=64, batch=FakeBatch(budget=10, sizes=sizes, steps=steps))
+    log = io.StringIO()
+    serve(reqs, srv, log=log)
+    recs = [json.loads(x) for x in log.getvalue().splitlines()]
+    assert sorted(r["request"] for r in recs) == list(range(5))
+    for r in recs:
+        q = reqs[r["request"]]
+        assert r == json.loads(json.dumps(request_record(q)))
+        assert r["latency_s"] == pytest.approx(q.completed - q.arrival) and r["queued_s"] >= 0
