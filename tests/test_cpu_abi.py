@@ -132,3 +132,12 @@ def test_integration_snippets_compile_against_the_header(tmp_path):
         cmd += ["-c", "-o", str(tmp_path / "snippet.o")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_integration_guide_covers_every_entry_point():
+    """Every function include/tcsem.h declares is described in INTEGRATION.md."""
+    from tcsem_fdtd_gb300.api import HEADER, declared_functions
+
+    doc = open(os.path.join(os.path.dirname(HEADER), "..", "INTEGRATION.md")).read()
+    missing = [f for f in declared_functions() if f not in doc]
+    assert not missing, missing
