@@ -673,6 +673,7 @@ template <typename T> struct SimImpl : SimBase {
     void select(int t) override {
         if (t < 0 || t >= (int)model.in.tx.size()) throw Error(TCSEM_ERR_INVALID, "transmitter index out of range");
         if (t == itx) return;
+        CK(cudaStreamSynchronize(stream));  // steps still in flight read the tables replaced below
         const Model &m = model;
         // sources
         std::vector<SourceSegment> segs = m.sources(t, opts.fix_dual_bipole != 0);
@@ -1016,6 +1017,8 @@ template <typename T> struct SimImpl : SimBase {
         if (!same) fail(TCSEM_ERR_INVALID, other);
         try {
             begin(h.itx);  // the transmitter's tables (receiver buffers) and a zero state, then the saved arrays
+            // the zeroing runs on the handle's (non-blocking) stream: let it finish before the copies
+            CK(cudaStreamSynchronize(stream));
         } catch (...) {
             std::fclose(f);
             throw;
