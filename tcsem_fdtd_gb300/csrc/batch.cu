@@ -87,7 +87,8 @@ template <typename T> struct BatchImpl : BatchBase {
         CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         counters.alloc(kMaxSlots * sizeof(int));
-        CK(cudaMemset(counters.p, 0, counters.n));
+        CK(cudaMemsetAsync(counters.p, 0, counters.n, stream));
+        CK(cudaStreamSynchronize(stream));
         for (int p = 0; p < 2; p++) {
             dsw[p].alloc(kMaxSlots * sizeof(SweepSlot<T>));
             dbs[p].alloc(kMaxSlots * sizeof(BoundarySlot<T>));
@@ -184,12 +185,14 @@ template <typename T> struct BatchImpl : BatchBase {
             smem_bnd[2] = std::max(smem_bnd[2], bb.smem_inv);
             nmax = std::max(nmax, m.g.N);
         }
+        // on the batch's (non-blocking) stream, finished before the next launch reads the tables
         for (int p = 0; p < 2 && n; p++) {
-            CK(cudaMemcpy(dsw[p].p, hsw[p].data(), n * sizeof(SweepSlot<T>), cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(dbs[p].p, hbs[p].data(), n * sizeof(BoundarySlot<T>), cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(drs[p].p, hrs[p].data(), n * sizeof(RxSlot<T>), cudaMemcpyHostToDevice));
+            CK(cudaMemcpyAsync(dsw[p].p, hsw[p].data(), n * sizeof(SweepSlot<T>), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(dbs[p].p, hbs[p].data(), n * sizeof(BoundarySlot<T>), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(drs[p].p, hrs[p].data(), n * sizeof(RxSlot<T>), cudaMemcpyHostToDevice, stream));
         }
-        CK(cudaMemcpy(counters.p, hc.data(), kMaxSlots * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpyAsync(counters.p, hc.data(), kMaxSlots * sizeof(int), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
         dirty = false;
         lps = 6 + (ilow.total() > 0 ? 1 : 0);
         if (!n) return;
@@ -307,6 +310,7 @@ template <typename T> struct BatchImpl : BatchBase {
             const ZChunks &zc = s.sim->zc;
             o->zchunks = zc.n;
             o->top_planes = zc.n > 1 && zc.kb[1] != (int)(s.sim->model.N / zc.n) ? zc.kb[1] : 0;
+            o->uploaded_bytes = s.sim->uploaded_bytes;
         }
         if (steps_done) *steps_done = s.done;
     }

@@ -112,6 +112,7 @@ struct SimBase {
     bool begun = false;
     long step = 0;
     size_t dev_bytes = 0;
+    size_t uploaded_bytes = 0;  // host-to-device bytes of the setup (tables, conductivity)
     int launches_per_step = 0;
     int chunks_used = 0, top_used = 0;  // z-chunk layout of the sweep in use (top_used 0: an even split)
     int tot_chunks_min = 0;             // chunk totals to allocate room for at least (a batch's tuner)
@@ -218,10 +219,28 @@ template <typename T> struct SimImpl : SimBase {
                 fld[b][5].as<T>()};
     }
 
+    // Copies between the host and the handle's memory go through the handle's stream and
+    // finish before returning: the kernels run on non-blocking streams, which a copy on the
+    // legacy default stream would not be ordered against (and a pageable host-to-device
+    // cudaMemcpy may return before its DMA lands).
+    void h2d(void *dst, const void *src, size_t n) {
+        if (!n) return;
+        CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+    void d2h(void *dst, const void *src, size_t n) {
+        if (!n) return;
+        CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+    void dzero(void *dst, size_t n) {
+        if (n) CK(cudaMemsetAsync(dst, 0, n, stream));
+    }
     template <class U> void upload(DevMem &m, const std::vector<U> &v) {
         m.alloc(v.size() * sizeof(U));
         dev_bytes += m.n;
-        if (!v.empty()) CK(cudaMemcpy(m.p, v.data(), m.n, cudaMemcpyHostToDevice));
+        uploaded_bytes += m.n;
+        h2d(m.p, v.data(), m.n);
     }
     template <class U> std::vector<T> conv(const std::vector<U> &v) { return std::vector<T>(v.begin(), v.end()); }
 
@@ -437,15 +456,15 @@ template <typename T> struct SimImpl : SimBase {
         }
         errw.alloc(sizeof(int));
         dev_bytes += sizeof(int);
-        CK(cudaMemset(errw.p, 0, sizeof(int)));
+        dzero(errw.p, sizeof(int));
         CK(sweep_configure<T>(g.N));
     }
     void check_error() override { check_device_error(); }
     void check_device_error() {
         int h = 0;
-        CK(cudaMemcpy(&h, errw.p, sizeof(int), cudaMemcpyDeviceToHost));
+        d2h(&h, errw.p, sizeof(int));
         if (h) {
-            CK(cudaMemset(errw.p, 0, sizeof(int)));
+            dzero(errw.p, sizeof(int));
             if (h == TCSEM_CHECK_CODE)
                 throw Error(TCSEM_ERR_CUDA, "a kernel index fell outside its array (bounds-checked build)");
             throw Error(TCSEM_ERR_CUDA, "a bounded wait in a kernel gave up (a bulk copy did not arrive)");
@@ -811,7 +830,7 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaStreamSynchronize(stream));
         check_device_error();
         std::vector<T> h(efs.n / sizeof(T));
-        CK(cudaMemcpy(h.data(), efs.p, efs.n, cudaMemcpyDeviceToHost));
+        d2h(h.data(), efs.p, efs.n);
         bool finite = true;
         for (size_t q = 0; q < h.size(); q++) { out[q] = (double)h[q]; finite &= std::isfinite(out[q]); }
         if (!finite) throw Error(TCSEM_ERR_NUMERIC, "non-finite receiver samples");
@@ -909,7 +928,7 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaStreamSynchronize(stream));
         size_t n = (size_t)model.NComp * rd.nr;
         std::vector<T> h(n);
-        CK(cudaMemcpy(h.data(), ef0.as<T>() + (size_t)slot * n, n * sizeof(T), cudaMemcpyDeviceToHost));
+        d2h(h.data(), ef0.as<T>() + (size_t)slot * n, n * sizeof(T));
         for (size_t q = 0; q < n; q++) values[q] = (double)h[q];
     }
 
@@ -927,7 +946,7 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaStreamSynchronize(stream));
         DevMem &dm = field_mem(comp, cur);
         std::vector<T> buf((size_t)g.total());
-        CK(cudaMemcpy(buf.data(), dm.p, buf.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        d2h(buf.data(), dm.p, buf.size() * sizeof(T));
         size_t q = 0;
         for (int k = 0; k < nz; k++)
             for (int j = 0; j < ny; j++)
@@ -939,18 +958,18 @@ template <typename T> struct SimImpl : SimBase {
         CK(cudaStreamSynchronize(stream));
         DevMem &dm = field_mem(comp, cur);
         std::vector<T> buf((size_t)g.total());
-        CK(cudaMemcpy(buf.data(), dm.p, buf.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        d2h(buf.data(), dm.p, buf.size() * sizeof(T));
         size_t q = 0;
         for (int k = 0; k < nz; k++)
             for (int j = 0; j < ny; j++)
                 for (int i = 0; i < nx; i++) buf[g.at(i, j, k + z0)] = (T)h[q++];
-        CK(cudaMemcpy(dm.p, buf.data(), buf.size() * sizeof(T), cudaMemcpyHostToDevice));
+        h2d(dm.p, buf.data(), buf.size() * sizeof(T));
         if (comp != TCSEM_CON) {  // keep the other buffer consistent for the fused sweep's untouched cells
             DevMem &other = field_mem(comp, cur ^ 1);
-            CK(cudaMemcpy(other.p, buf.data(), buf.size() * sizeof(T), cudaMemcpyHostToDevice));
+            h2d(other.p, buf.data(), buf.size() * sizeof(T));
         }
         if (comp == TCSEM_BZ)  // a plain Bz plane: no chunk offsets
-            for (int b = 0; b < 2; b++) CK(cudaMemset(tot[b].p, 0, tot[b].n));
+            for (int b = 0; b < 2; b++) dzero(tot[b].p, tot[b].n);
     }
 
     // ---- checkpoint of a run in progress: what one step hands the next (the field set the
@@ -981,7 +1000,7 @@ template <typename T> struct SimImpl : SimBase {
         bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
         auto put = [&](const void *dev, size_t n) {
             buf.resize(n);
-            if (n) CK(cudaMemcpy(buf.data(), dev, n, cudaMemcpyDeviceToHost));
+            d2h(buf.data(), dev, n);
             ok = ok && std::fwrite(buf.data(), 1, n, f) == n;
         };
         try {
@@ -1027,7 +1046,7 @@ template <typename T> struct SimImpl : SimBase {
         auto get = [&](void *dev, size_t n) {
             buf.resize(n);
             ok = ok && std::fread(buf.data(), 1, n, f) == n;
-            if (ok && n) CK(cudaMemcpy(dev, buf.data(), n, cudaMemcpyHostToDevice));
+            if (ok) h2d(dev, buf.data(), n);
         };
         try {
             for (int c = 0; c < 6; c++) get(fld[h.cur][c].p, (size_t)h.field_bytes);
@@ -1044,7 +1063,7 @@ template <typename T> struct SimImpl : SimBase {
             throw Error(TCSEM_ERR_IO, std::string(path) + " is truncated");
         }
         const int s = (int)h.step;
-        CK(cudaMemcpy(gate_base.p, &s, sizeof(int), cudaMemcpyHostToDevice));
+        h2d(gate_base.p, &s, sizeof(int));
         cur = h.cur;
         step = h.step;
     }
