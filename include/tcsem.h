@@ -73,6 +73,8 @@ typedef struct {
     int launches_per_step; /* kernels launched per time step by tcsem_advance */
     int zchunks;          /* z-chunks of the fused sweep in use */
     int top_planes;       /* planes of the top z-chunk when it runs beside the others, else 0 */
+    size_t uploaded_bytes; /* host-to-device bytes the open copied (conductivity, grid, boundary and
+                              step tables); the fields start as zero on the device */
 } tcsem_info;
 
 /* Opening a survey.  tcsem_open_dir reads FDTD_setup.in, Cond.bin, Receiver.in
@@ -80,6 +82,52 @@ typedef struct {
  * directory (ModelingSetup.cpp:43-209, LoadRxTxPos.cpp:43-200). */
 void tcsem_default_opts(tcsem_opts *opts);
 tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t **out);
+
+/* In-memory open: the same survey from host buffers, for a host that already
+ * holds the model and the survey (the reference's ModelingSetup and
+ * LoadRxTxPos, ModelingSetup.cpp:34-234 and LoadRxTxPos.cpp:35-200, fill the
+ * same values from the four files).  The fields of tcsem_model are the eight
+ * lines of FDTD_setup.in in file order plus the conductivity of Cond.bin;
+ * those of tcsem_survey are Receiver.in and Transmitter.in (transmitter t has
+ * id t+1, receiver r has id r+1; angles in degrees, as in the file).  Every
+ * buffer is copied during the call.  The checks and error codes are those of
+ * tcsem_open_dir: TCSEM_ERR_PARSE for what would be a malformed file (an
+ * orientation outside 1..5, a receiver id out of range, no receivers),
+ * TCSEM_ERR_INVALID for an inconsistent grid. */
+typedef struct {
+    double sfa1, sfa2;               /* line 1: factors of the time step and of gamma */
+    int n1;                          /* line 2: source samples (nsrc = n1/2) ... */
+    double sita_t;                   /*         ... and the width of the Gaussian source pulse */
+    double x0, y0, z0;               /* line 3: origin of the grid */
+    double dxmin, dymin, dzmin;      /* line 4: core cell sizes */
+    double arg1, arg2;               /* line 5: growth factors of the boundary strips */
+    int ALx2, ALx1, Nx, ARx1, ARx2;  /* line 6: cells along x */
+    int Ay2, Ay1, Ny;                /* line 7: cells along y */
+    int Az2, Az1, Nz;                /* line 8: cells along z */
+    const double *con;               /* Cond.bin: conductivity (S/m) [N][M][L], x fastest */
+} tcsem_model;
+
+typedef struct {
+    int ort;                          /* 1 x, 2 y, 3 z, 4 azimuth/dip, 5 two bipoles (LoadRxTxPos.cpp:151-200) */
+    double len, x, y, z;              /* bipole length and centre */
+    double azi, dip;                  /* degrees (ort 4 and 5) */
+    double len1, x1, y1, z1, azi1, dip1; /* second bipole (ort 5) */
+    int nr;                           /* receivers of this transmitter ... */
+    const int *rx;                    /* ... their ids, 1..NRx, in output order */
+} tcsem_transmitter;
+
+typedef struct {
+    double T0, Tn;             /* Receiver.in line 1: first and last sampling time */
+    int Nt, IsLog;             /* line 2: samples, log (1) or linear (0) spacing */
+    int comps[6];              /* line 3: record Ex Ey Ez Bx By Bz */
+    int NRx;                   /* receivers */
+    const double *rx_xyz;      /* [NRx][3] positions */
+    int NTx;                   /* transmitters */
+    const tcsem_transmitter *tx;
+} tcsem_survey;
+
+tcsem_status tcsem_open(const tcsem_model *model, const tcsem_survey *survey, const tcsem_opts *opts,
+                        tcsem_sim_t **out);
 tcsem_status tcsem_close(tcsem_sim_t *sim);
 const char *tcsem_last_error(const tcsem_sim_t *sim); /* message of the last failed call on `sim` */
 const char *tcsem_open_error(void);                   /* message of the last failed open (per thread) */
@@ -199,7 +247,10 @@ tcsem_status tcsem_batch_stats(tcsem_batch_t *batch, int *slots, int *running, s
  *
  * The first call on each device, with that device current, looks up the
  * array's address with cudaGetSymbolAddress and keeps it; make that first call
- * before any stream capture.  Nothing in the scratch has to start at zero:
+ * before any stream capture.  The address belongs to the device's primary
+ * context: after cudaDeviceReset (or anything else that destroys that context)
+ * the kept address is stale, so do not call this entry point again in the same
+ * process after a reset.  Nothing in the scratch has to start at zero:
  * every element a call reads is written earlier in the same call.  There is
  * one scratch per device, shared by all handles: calls that can overlap on a
  * device (different handles, threads or streams) race on it, so the caller

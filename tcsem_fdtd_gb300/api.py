@@ -36,7 +36,29 @@ class Info(C.Structure):
     _fields_ = [("L", C.c_int), ("M", C.c_int), ("N", C.c_int), ("L1", C.c_int), ("M1", C.c_int),
                 ("NRx", C.c_int), ("NTx", C.c_int), ("Nt", C.c_int), ("NComp", C.c_int), ("nefcmp", C.c_int),
                 ("nsteps", C.c_long), ("precision", C.c_int), ("device_bytes", C.c_size_t),
-                ("launches_per_step", C.c_int), ("zchunks", C.c_int), ("top_planes", C.c_int)]
+                ("launches_per_step", C.c_int), ("zchunks", C.c_int), ("top_planes", C.c_int),
+                ("uploaded_bytes", C.c_size_t)]
+
+
+# records of the in-memory open (tcsem_model / tcsem_transmitter / tcsem_survey)
+MODEL_FIELDS = ["sfa1", "sfa2", "n1", "sita_t", "x0", "y0", "z0", "dxmin", "dymin", "dzmin", "arg1", "arg2",
+                "ALx2", "ALx1", "Nx", "ARx1", "ARx2", "Ay2", "Ay1", "Ny", "Az2", "Az1", "Nz"]
+
+
+class ModelRec(C.Structure):
+    _fields_ = [(f, C.c_int if f in ("n1", "ALx2", "ALx1", "Nx", "ARx1", "ARx2", "Ay2", "Ay1", "Ny", "Az2", "Az1",
+                                   "Nz") else C.c_double) for f in MODEL_FIELDS] + [("con", C.POINTER(C.c_double))]
+
+
+class TxRec(C.Structure):
+    _fields_ = [("ort", C.c_int)] + [(f, C.c_double) for f in ("len", "x", "y", "z", "azi", "dip", "len1", "x1",
+                                                                 "y1", "z1", "azi1", "dip1")] + \
+        [("nr", C.c_int), ("rx", C.POINTER(C.c_int))]
+
+
+class SurveyRec(C.Structure):
+    _fields_ = [("T0", C.c_double), ("Tn", C.c_double), ("Nt", C.c_int), ("IsLog", C.c_int), ("comps", C.c_int * 6),
+                ("NRx", C.c_int), ("rx_xyz", C.POINTER(C.c_double)), ("NTx", C.c_int), ("tx", C.POINTER(TxRec))]
 
 
 def declared_functions():
@@ -61,6 +83,7 @@ def library():
     sig = {
         "tcsem_default_opts": (None, [C.POINTER(Opts)]),
         "tcsem_open_dir": (i, [C.c_char_p, C.POINTER(Opts), C.POINTER(vp)]),
+        "tcsem_open": (i, [C.POINTER(ModelRec), C.POINTER(SurveyRec), C.POINTER(Opts), C.POINTER(vp)]),
         "tcsem_close": (i, [vp]),
         "tcsem_last_error": (C.c_char_p, [vp]),
         "tcsem_open_error": (C.c_char_p, []),
@@ -123,11 +146,49 @@ def _dptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-class Simulation:
-    """One survey on one GPU: the handle of include/tcsem.h."""
+def memory_records(model, survey):
+    """tcsem_model / tcsem_survey records for tcsem_open from plain values.
 
-    def __init__(self, directory, precision=32, device=0, fix_dual_bipole=False, graph_steps=0, zchunks=0,
-                 serial_boundary=False, top_planes=0, padded_plane=False):
+    model:  the FDTD_setup.in fields of MODEL_FIELDS plus ``con`` (conductivity [N][M][L]);
+    survey: ``T0 Tn Nt IsLog comps`` (Receiver.in), ``rx_xyz`` ([NRx][3]) and ``tx``, a list of
+            dicts with ``ort len x y z`` (+ ``azi dip`` in degrees for ort 4/5, + ``len1 x1 y1 z1
+            azi1 dip1`` for ort 5) and ``rx`` (1-based receiver ids).
+    Returns (model record, survey record, arrays the records point into)."""
+    keep = []
+    m = ModelRec()
+    for f in MODEL_FIELDS:
+        setattr(m, f, model[f])
+    con = np.ascontiguousarray(model["con"], dtype=np.float64)
+    keep.append(con)
+    m.con = _dptr(con)
+    s = SurveyRec()
+    s.T0, s.Tn, s.Nt, s.IsLog = survey["T0"], survey["Tn"], survey["Nt"], survey["IsLog"]
+    s.comps[:] = [int(v) for v in survey["comps"]]
+    xyz = np.ascontiguousarray(survey["rx_xyz"], dtype=np.float64).reshape(-1, 3)
+    keep.append(xyz)
+    s.NRx, s.rx_xyz = xyz.shape[0], _dptr(xyz)
+    txs = (TxRec * len(survey["tx"]))()
+    for q, t in enumerate(survey["tx"]):
+        r = txs[q]
+        r.ort = int(t["ort"])
+        for f in ("len", "x", "y", "z", "azi", "dip", "len1", "x1", "y1", "z1", "azi1", "dip1"):
+            setattr(r, f, float(t.get(f, 0.0)))
+        ids = np.ascontiguousarray(t["rx"], dtype=np.int32)
+        keep.append(ids)
+        r.nr, r.rx = len(ids), ids.ctypes.data_as(C.POINTER(C.c_int))
+    keep.append(txs)
+    s.NTx, s.tx = len(survey["tx"]), txs
+    return m, s, keep
+
+
+class Simulation:
+    """One survey on one GPU: the handle of include/tcsem.h.
+
+    Opened from a survey directory (tcsem_open_dir), or with ``model=`` and ``survey=`` from
+    host values (tcsem_open, see :func:`memory_records`)."""
+
+    def __init__(self, directory=None, precision=32, device=0, fix_dual_bipole=False, graph_steps=0, zchunks=0,
+                 serial_boundary=False, top_planes=0, padded_plane=False, model=None, survey=None):
         L = library()
         o = Opts()
         L.tcsem_default_opts(C.byref(o))
@@ -137,7 +198,11 @@ class Simulation:
         o.top_planes = top_planes
         o.padded_plane = int(padded_plane)  # 0, 1 (powers of two) or 2 (5-smooth lengths)
         h = C.c_void_p()
-        st = L.tcsem_open_dir(os.fsencode(directory), C.byref(o), C.byref(h))
+        if directory is not None:
+            st = L.tcsem_open_dir(os.fsencode(directory), C.byref(o), C.byref(h))
+        else:
+            mrec, srec, _keep = memory_records(model, survey)
+            st = L.tcsem_open(C.byref(mrec), C.byref(srec), C.byref(o), C.byref(h))
         if st != 0:
             raise TcsemError(st, L.tcsem_open_error().decode())
         self._h = h

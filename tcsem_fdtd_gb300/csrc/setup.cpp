@@ -168,6 +168,52 @@ SurveyInput read_survey_dir(const std::string &dir) {
     return in;
 }
 
+// The same SurveyInput from host records (tcsem_open): the values and checks of
+// read_survey_dir, field for field, with angles converted from degrees as the
+// parser does (LoadRxTxPos.cpp:151-200).
+SurveyInput survey_from_host(const tcsem_model *m, const tcsem_survey *s) {
+    if (!m || !s) throw Error(TCSEM_ERR_INVALID, "null model or survey");
+    SurveyInput in;
+    in.sfa1 = m->sfa1; in.sfa2 = m->sfa2; in.n1 = m->n1; in.sita_t = m->sita_t;
+    in.x0 = m->x0; in.y0 = m->y0; in.z0 = m->z0;
+    in.dxmin = m->dxmin; in.dymin = m->dymin; in.dzmin = m->dzmin;
+    in.arg1 = m->arg1; in.arg2 = m->arg2;
+    in.ALx2 = m->ALx2; in.ALx1 = m->ALx1; in.Nx = m->Nx; in.ARx1 = m->ARx1; in.ARx2 = m->ARx2;
+    in.Ay2 = m->Ay2; in.Ay1 = m->Ay1; in.Ny = m->Ny;
+    in.Az2 = m->Az2; in.Az1 = m->Az1; in.Nz = m->Nz;
+    long L = in.ALx2 + in.ALx1 + in.ARx2 + in.ARx1 + in.Nx, M = 2 * (in.Ay2 + in.Ay1) + in.Ny, N = in.Nz + in.Az2 + in.Az1;
+    if (L < 1 || M < 1 || N < 1 || L * M * N > (1L << 33)) throw Error(TCSEM_ERR_INVALID, "bad grid dimensions");
+    if (!m->con) throw Error(TCSEM_ERR_INVALID, "null conductivity");
+    in.con.assign(m->con, m->con + (size_t)L * M * N);
+    in.T0 = s->T0; in.Tn = s->Tn; in.Nt = s->Nt; in.IsLog = s->IsLog;
+    for (int c = 0; c < 6; c++) in.isComp[c] = s->comps[c];
+    if (s->NRx < 1 || !s->rx_xyz) throw Error(TCSEM_ERR_PARSE, "survey: no receivers");
+    in.rx.resize(s->NRx); in.ry.resize(s->NRx); in.rz.resize(s->NRx);
+    for (int r = 0; r < s->NRx; r++) {
+        in.rx[r] = s->rx_xyz[3 * r]; in.ry[r] = s->rx_xyz[3 * r + 1]; in.rz[r] = s->rx_xyz[3 * r + 2];
+    }
+    if (s->NTx < 1 || !s->tx) throw Error(TCSEM_ERR_PARSE, "survey: no transmitters");
+    in.tx.assign(s->NTx, Transmitter());
+    for (int q = 0; q < s->NTx; q++) {
+        const tcsem_transmitter &h = s->tx[q];
+        Transmitter &T = in.tx[q];
+        T.ort = h.ort;
+        T.len = h.len; T.x = h.x; T.y = h.y; T.z = h.z;
+        if (T.ort < 1 || T.ort > 5) throw Error(TCSEM_ERR_PARSE, "survey: illegal transmitter orientation");
+        if (T.ort >= 4) { T.azi = h.azi * kPi / 180.0; T.dip = h.dip * kPi / 180.0; }
+        if (T.ort == 5) {
+            T.len1 = h.len1; T.x1 = h.x1; T.y1 = h.y1; T.z1 = h.z1;
+            T.azi1 = h.azi1 * kPi / 180.0; T.dip1 = h.dip1 * kPi / 180.0;
+        }
+        T.nr = h.nr;
+        if (T.nr < 1 || !h.rx) throw Error(TCSEM_ERR_PARSE, "survey: no receivers for a transmitter");
+        T.rx.assign(h.rx, h.rx + T.nr);
+        for (int id : T.rx)
+            if (id < 1 || id > s->NRx) throw Error(TCSEM_ERR_PARSE, "survey: receiver id out of range");
+    }
+    return in;
+}
+
 // ---------------------------------------------------------------- model build
 
 namespace {

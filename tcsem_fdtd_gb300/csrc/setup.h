@@ -11,6 +11,8 @@
 #include <stdexcept>
 #include <cstdint>
 
+#include "tcsem.h"
+
 namespace tcsem {
 
 struct Error : std::runtime_error {
@@ -44,6 +46,8 @@ struct SurveyInput {
 };
 
 SurveyInput read_survey_dir(const std::string &dir);
+// the same from the host records of the in-memory open (tcsem_open)
+SurveyInput survey_from_host(const tcsem_model *m, const tcsem_survey *s);
 
 // Source injection as a set of axis-aligned segments: E component `comp`
 // (0 Ex, 1 Ey, 2 Ez), fixed cell along the other two axes, `count` cells from

@@ -57,17 +57,8 @@ template <class F> static tcsem_status guard(tcsem_sim_t *s, F &&f) {
     }
 }
 
-extern "C" {
-
-void tcsem_default_opts(tcsem_opts *o) {
-    if (!o) return;
-    std::memset(o, 0, sizeof *o);
-    o->precision = TCSEM_FP32;
-}
-
-tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t **out) {
-    NvtxRange nr("tcsem_open_dir");
-    if (!dir || !out) { g_open_err = "null argument"; return TCSEM_ERR_INVALID; }
+// the survey of `read` (files or host records) set up on the device
+template <class F> static tcsem_status open_impl(F &&read, const tcsem_opts *opts, tcsem_sim_t **out) {
     *out = nullptr;
     tcsem_opts o;
     tcsem_default_opts(&o);
@@ -80,7 +71,7 @@ tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t
         else impl.reset(new SimImpl<float>());
         impl->opts = o;
         impl->device = o.device;
-        impl->model.build(read_survey_dir(dir));
+        impl->model.build(read());
         impl->sched = impl->model.schedule();
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device || o.device < 0)
@@ -100,6 +91,27 @@ tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t
         g_open_err = e.what();
         return TCSEM_ERR_INVALID;
     }
+}
+
+extern "C" {
+
+void tcsem_default_opts(tcsem_opts *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->precision = TCSEM_FP32;
+}
+
+tcsem_status tcsem_open_dir(const char *dir, const tcsem_opts *opts, tcsem_sim_t **out) {
+    NvtxRange nr("tcsem_open_dir");
+    if (!dir || !out) { g_open_err = "null argument"; return TCSEM_ERR_INVALID; }
+    return open_impl([&] { return read_survey_dir(dir); }, opts, out);
+}
+
+tcsem_status tcsem_open(const tcsem_model *model, const tcsem_survey *survey, const tcsem_opts *opts,
+                        tcsem_sim_t **out) {
+    NvtxRange nr("tcsem_open");
+    if (!model || !survey || !out) { g_open_err = "null argument"; return TCSEM_ERR_INVALID; }
+    return open_impl([&] { return survey_from_host(model, survey); }, opts, out);
 }
 
 const char *tcsem_open_error(void) { return g_open_err.c_str(); }
@@ -125,6 +137,7 @@ tcsem_status tcsem_get_info(const tcsem_sim_t *s, tcsem_info *o) {
     o->launches_per_step = b.launches_per_step;
     o->zchunks = b.chunks_used;
     o->top_planes = b.top_used;
+    o->uploaded_bytes = b.uploaded_bytes;
     return TCSEM_OK;
 }
 

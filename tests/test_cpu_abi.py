@@ -35,16 +35,18 @@ def test_opts_and_info_struct_layout_matches_header():
 
 
 def test_struct_offsets_match_the_c_compiler(tmp_path):
-    """Every field of tcsem_opts / tcsem_info sits where gcc puts it for include/tcsem.h."""
+    """Every field of the records in include/tcsem.h sits where gcc puts it."""
     import shutil
     import subprocess
 
-    from tcsem_fdtd_gb300.api import HEADER, Info, Opts
+    from tcsem_fdtd_gb300.api import HEADER, Info, ModelRec, Opts, SurveyRec, TxRec
 
     if not shutil.which("gcc"):
         pytest.skip("gcc not found")
     lines = []
-    for st, cname in ((Opts, "tcsem_opts"), (Info, "tcsem_info")):
+    records = ((Opts, "tcsem_opts"), (Info, "tcsem_info"), (ModelRec, "tcsem_model"), (TxRec, "tcsem_transmitter"),
+               (SurveyRec, "tcsem_survey"))
+    for st, cname in records:
         lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
         for f, _ in st._fields_:
             lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
@@ -57,7 +59,7 @@ def test_struct_offsets_match_the_c_compiler(tmp_path):
     for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
         cname, f, v = ln.split()
         got[(cname, f)] = int(v)
-    for st, cname in ((Opts, "tcsem_opts"), (Info, "tcsem_info")):
+    for st, cname in records:
         assert got[(cname, "sizeof")] == C.sizeof(st), cname
         for f, _ in st._fields_:
             assert got[(cname, f)] == getattr(st, f).offset, (cname, f)
@@ -78,6 +80,41 @@ def test_open_without_gpu_or_with_bad_inputs_fails_loudly(case_dir, tmp_path):
         with pytest.raises(t.TcsemError) as e:
             t.Simulation(case_dir("tiny"))
         assert e.value.status == 4  # TCSEM_ERR_CUDA, never a silent CPU path
+
+
+def test_in_memory_open_checks_its_records_like_the_parser():
+    """tcsem_open refuses what tcsem_open_dir refuses in a file, with the same codes, before it
+    touches a GPU; a valid survey then stops at the device (TCSEM_ERR_CUDA without a GPU)."""
+    import copy
+
+    import tcsem_fdtd_gb300 as t
+    from tcsem_fdtd_gb300 import inputs
+
+    model, survey = inputs.memory_case(inputs.case("txvar"))
+    bad = copy.deepcopy(survey)
+    bad["tx"][2]["ort"] = 7
+    with pytest.raises(t.TcsemError) as e:
+        t.Simulation(model=model, survey=bad)
+    assert e.value.status == 2 and "orientation" in str(e.value)
+    bad = copy.deepcopy(survey)
+    bad["tx"][0]["rx"] = [1, 6]  # five receivers
+    with pytest.raises(t.TcsemError) as e:
+        t.Simulation(model=model, survey=bad)
+    assert e.value.status == 2 and "receiver id" in str(e.value)
+    m2 = dict(model, ALx1=0, ALx2=0)
+    with pytest.raises(t.TcsemError) as e:
+        t.Simulation(model=m2, survey=survey)
+    assert e.value.status == 3
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        with pytest.raises(t.TcsemError) as e:
+            t.Simulation(model=model, survey=survey)
+        assert e.value.status == 4 and "CUDA device" in str(e.value)
 
 
 def test_parse_errors_are_reported(tmp_path):
