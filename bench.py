@@ -271,6 +271,7 @@ def main():
     ap.add_argument("--workload", default="marine3d_256x256x160")
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="leave out the batched and served sub-records")
     ap.add_argument("--surveys", type=int, default=64, help="batch64: surveys in the batch; serve_poisson: requests")
     ap.add_argument("--rate", type=float, default=8.0, help="serve_poisson: mean request arrivals per second")
     args = ap.parse_args()
@@ -286,6 +287,76 @@ def main():
         dist.close()
 
 
+def timed_steps(d, precision, device, warmup, steps):
+    """Device time of `steps` steps of the production loop: the handle captures blocks of
+    `steps` steps (64 for longer runs) as one CUDA graph, so the timed region is graph
+    replays; after `warmup` steps and one untimed replay (the graph's first launch uploads it)."""
+    from tcsem_fdtd_gb300 import Simulation
+
+    gsteps = steps - steps % 2 if steps < 64 else 64
+    sim = Simulation(d, precision=precision, device=device, graph_steps=max(2, gsteps))
+    sim.begin(0)
+    sim.advance(warmup)
+    sim.advance(steps)  # untimed replay
+    sim.synchronize()
+    return sim, gsteps
+
+
+def batched_record(precision, device, surveys=16):
+    """A compact batched-form record: `surveys` generated surveys of the batched workload
+    (96..192 x 96..192 x 96..128 cells, 1 s window) as one device batch against the same
+    surveys run one at a time, end to end (setup, all steps, traces to the host)."""
+    from tcsem_fdtd_gb300 import Batch, Simulation, inputs
+
+    root = tempfile.mkdtemp(prefix="tcsem_bench_batch_")
+    dirs = []
+    for q in range(surveys):
+        dd = os.path.join(root, f"s{q:03d}")
+        inputs.write_case(inputs.batch_case(q), dd)
+        dirs.append(dd)
+    cells_steps = 0
+    t0 = time.perf_counter()
+    for dd in dirs:
+        with Simulation(dd, precision=precision, device=device) as sim:
+            sim.run(0)
+            i = sim.info
+            cells_steps += i["L"] * i["M"] * i["N"] * i["nsteps"]
+    tp = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    with Batch(precision=precision, device=device) as b:
+        slots = [b.add(dd) for dd in dirs]
+        while b.stats()["running"]:
+            b.advance(256)
+        b.poll()
+        for sl in slots:
+            b.traces(sl)
+    tb = time.perf_counter() - t0
+    return {"surveys": surveys, "grids": "96..192 x 96..192 x 96..128", "window_s": 1.0,
+            "sims_per_hour": 3600.0 * surveys / tb, "plain_sims_per_hour": 3600.0 * surveys / tp,
+            "vs_plain": tp / tb, "batched_s": tb, "plain_s": tp,
+            "Gcell_steps_per_s": {"batched": cells_steps / tb / 1e9, "plain": cells_steps / tp / 1e9}}
+
+
+def served_record(precision, device, requests=24, rate=8.0):
+    """A compact served-form record: a seeded Poisson stream of `requests` survey requests
+    (64x64x48 .. 256x256x160 cells, 1 s or 10 s windows) at `rate` per second, served with
+    continuous batching and one at a time (sims/hr, p50/p99 latency)."""
+    from tcsem_fdtd_gb300 import serve as sv
+
+    reqs = sv.make_stream(requests, rate, 5, tn=(1.0, 10.0))
+    srv = sv.Server(precision=precision, device=device, budget=64 << 30, block=64)
+    try:
+        batched = sv.summary(reqs, sv.serve(reqs, srv))
+    finally:
+        srv.close()
+    plain_reqs = [sv.Request(r.rid, r.directory, r.arrival) for r in reqs]
+    plain = sv.summary(plain_reqs, sv.run_plain(plain_reqs, precision=precision, device=device))
+    keys = ("sims_per_hour", "p50_latency_s", "p99_latency_s", "wall_s")
+    return {"requests": requests, "rate_per_s": rate, "sizes": "64x64x48 .. 256x256x160", "windows_s": [1.0, 10.0],
+            "batched": {k: batched[k] for k in keys}, "plain": {k: plain[k] for k in keys},
+            "vs_plain": batched["sims_per_hour"] / plain["sims_per_hour"]}
+
+
 def run_gb300(args, dist):
     from tcsem_fdtd_gb300 import Simulation, build, inputs
 
@@ -294,12 +365,9 @@ def run_gb300(args, dist):
     c = inputs.case(args.workload)
     g = inputs.grid_axes(c)
     cells = g["L"] * g["M"] * g["N"]
-    sim = Simulation(d, precision=args.precision, device=dist.local)
-    nsteps_total = sim.info["nsteps"]
-    K = min(args.steps, nsteps_total - args.warmup)
-    sim.begin(0)
-    sim.advance(args.warmup)  # warm-up steps (graph capture happens here)
-    sim.synchronize()
+    nsteps_total = inputs.steps_estimate(c)
+    K = max(2, min(args.steps, (nsteps_total - args.warmup) // 2 - 1))
+    sim, gsteps = timed_steps(d, args.precision, dist.local, args.warmup, K)
     dist.barrier()
     with ClockSampler(dist.local) as clk:
         ms = sim.timed_advance(K)
@@ -307,42 +375,59 @@ def run_gb300(args, dist):
     ms_max = dist.reduce(ms, "max")
     work = dist.reduce(cells * K, "sum")
     value = work / (ms_max * 1e-3) / 1e9
+    launches = K * sim.info["launches_per_step"] + math.ceil(K / gsteps)
     # per-kernel timings on the same stream (events around standalone launches)
     _, ms_sweep, ms_bnd = sim.time_steps(0, 64)
+    sim.close()
     algo = ALGO_BYTES_PER_CELL[args.precision] * cells
     peak, peak_kind = measured_peak()
     achieved = algo / (ms_sweep * 1e-3) / 1e9
-    # end to end through the C ABI: files -> device -> all steps -> traces on the host
+    # the same steps in the FP64 build (the reference's own precision)
+    other = 64 if args.precision == 32 else 32
+    sim2, _ = timed_steps(d, other, dist.local, args.warmup, K)
+    ms2 = dist.reduce(sim2.timed_advance(K), "max")
+    _, ms_sweep2, _ = sim2.time_steps(0, 64)
+    sim2.close()
+    other_rec = {"value": dist.reduce(cells * K, "sum") / (ms2 * 1e-3) / 1e9, "unit": "Gcell-steps/s",
+                 "ms_per_step": ms2 / K, "sweep_ms_per_launch": ms_sweep2,
+                 "sweep_frac": ALGO_BYTES_PER_CELL[other] * cells / (ms_sweep2 * 1e-3) / 1e9 / peak}
+    # end to end through the C ABI with host buffers: tcsem_open of the model and survey held in
+    # host memory (copied to the device inside), all steps, traces copied back to the host
+    model, survey = inputs.memory_case(c)
+    dist.barrier()
     t0 = time.perf_counter()
-    with Simulation(d, precision=args.precision, device=dist.local) as s2:
+    with Simulation(precision=args.precision, device=dist.local, model=model, survey=survey) as s2:
         tr = s2.run(0)
         info2 = s2.info
     e2e_s = time.perf_counter() - t0
     e2e_s = dist.reduce(e2e_s, "max")
     e2e_val = dist.reduce(cells * info2["nsteps"], "sum") / e2e_s / 1e9
-    h2d = info2["device_bytes"]
-    d2h = tr.nbytes
-    sim.close()
     line = {
         "metric": "Gcell-steps/s", "value": value, "unit": "Gcell-steps/s", "n_gpus": dist.world, "steps": K,
         "warmup": args.warmup, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
         "config": {"workload": args.workload, "grid": [g["L"], g["M"], g["N"]], "cells": cells,
                    "plane": [info2["L1"], info2["M1"]], "receivers": info2["NRx"],
-                   "steps_per_run": nsteps_total, "parallelism": f"replicas{dist.world}",
+                   "steps_per_run": info2["nsteps"], "parallelism": f"replicas{dist.world}",
+                   "timed": "%d steps as replays of a captured %d-step CUDA graph" % (K, gsteps),
                    "l2": "working set 13 x %.0f MB volume arrays > 129 MB L2, no flush needed"
                          % (cells * 4 * 1.13 / 1e6)},
-        "gpu_launches": K * info2["launches_per_step"] + math.ceil(K / 64),
+        "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_fused_sweep", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(args.workload), "ms_per_launch": ms_sweep,
                      "algo_bytes_per_launch": algo, "boundary_ms_per_step": ms_bnd},
-        "e2e": {"value": e2e_val, "unit": "Gcell-steps/s", "h2d_bytes_per_step": h2d / info2["nsteps"],
-                "d2h_bytes_per_step": d2h / info2["nsteps"],
-                "what": "tcsem_open_dir (files, host setup, uploads) + tcsem_run of all %d steps + traces to host"
-                        % info2["nsteps"], "seconds": e2e_s},
+        "e2e": {"value": e2e_val, "unit": "Gcell-steps/s",
+                "h2d_bytes_per_step": info2["uploaded_bytes"] / info2["nsteps"],
+                "d2h_bytes_per_step": tr.nbytes / info2["nsteps"],
+                "what": "tcsem_open of host buffers (conductivity, grid and survey; setup and uploads) + "
+                        "tcsem_run of all %d steps + traces to the host" % info2["nsteps"], "seconds": e2e_s},
         "clocks": clk.summary(),
+        ("fp64" if other == 64 else "fp32"): other_rec,
     }
+    if not args.no_forms:
+        line["batched"] = batched_record(args.precision, dist.local)
+        line["served"] = served_record(args.precision, dist.local)
     if dist.rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_reference(args, d, cells)

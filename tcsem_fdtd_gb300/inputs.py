@@ -267,10 +267,33 @@ CASES = {
         receivers=[(1500.0 + 500.0 * i, 0.0, 1000.0) for i in range(5)],
         transmitters=[dict(ort=1, len=200.0, x=0.0, y=0.0, z=600.0)],
     ),
+    # a grid three sweep tiles wide (142 = 2 x 64 + 14: a partial last x-tile) and five
+    # tile rows high (36 = 4 x 8 + 4), random conductivity, transmitters that cross the
+    # tile boundaries at i = 64 (x-directed) and j = 16 (y-directed), receivers spread
+    # over every tile; its 192 x 76 continuation plane keeps the oracle fast
+    "wide_142x36x25": _base(
+        dmin=(40.0, 40.0, 40.0), arg1=1.15, arg2=1.25, xsplit=(3, 8, 118, 10, 3), ysplit=(3, 8, 14),
+        zsplit=(3, 8, 14), n1=200, sita_t=1e-4, T0=1e-3, Tn=5e-2, Nt=24, comps=(1, 1, 1, 1, 1, 1),
+        model=dict(kind="random", seed=23, range=(0.05, 3.0)),
+        receivers=[(-2200.0 + 300.0 * i, 40.0 * (i % 4) - 60.0, 0.0 if i % 3 else 120.0) for i in range(16)],
+        transmitters=[dict(ort=1, len=200.0, x=-240.0, y=20.0, z=60.0),
+                      dict(ort=2, len=160.0, x=1100.0, y=-70.0, z=100.0),
+                      dict(ort=4, len=200.0, x=2330.0, y=-40.0, z=140.0, azi=35.0, dip=25.0)],
+    ),
     # survey config 1: homogeneous 1 S/m half-space, 64 x 64 x 48, 25 m, growth 1.15
     "halfspace_64x64x48": _base(
         dmin=(25.0, 25.0, 25.0), arg1=1.15, arg2=1.15, xsplit=(0, 12, 24, 28, 0), ysplit=(0, 20, 24),
         zsplit=(0, 28, 20), n1=200, sita_t=1e-5, sfa1=1.5, sfa2=2.0, T0=1e-4, Tn=1.0, Nt=61,
+        comps=(1, 1, 0, 0, 1, 1), model=dict(kind="uniform", sigma=1.0),
+        receivers=[(500.0 + 250.0 * i, 0.0, 0.0) for i in range(15)],
+        transmitters=[dict(ort=1, len=25.0, x=0.0, y=0.0, z=0.0)],
+    ),
+    # the same half-space survey refined two-fold: 12.5 m core cells and growth 1.075, so
+    # every cell near the receivers is about half its size in halfspace_64x64x48 (a 2 km
+    # offset sits in 136 m cells instead of 269 m), over about the same extents; 960 x 576 plane
+    "halfspace_refined_133x130x95": _base(
+        dmin=(12.5, 12.5, 12.5), arg1=1.075, arg2=1.075, xsplit=(0, 29, 48, 56, 0), ysplit=(0, 41, 48),
+        zsplit=(0, 55, 40), n1=200, sita_t=1e-5, sfa1=1.5, sfa2=2.0, T0=1e-4, Tn=1.0, Nt=61,
         comps=(1, 1, 0, 0, 1, 1), model=dict(kind="uniform", sigma=1.0),
         receivers=[(500.0 + 250.0 * i, 0.0, 0.0) for i in range(15)],
         transmitters=[dict(ort=1, len=25.0, x=0.0, y=0.0, z=0.0)],
@@ -297,6 +320,20 @@ CASES = {
     # survey config 3: 3-D marine model, 256 x 256 x 160 at 25 m
     "marine3d_256x256x160": _base(
         dmin=(25.0, 25.0, 25.0), arg1=1.08, arg2=1.08, xsplit=(0, 40, 176, 40, 0), ysplit=(0, 40, 176),
+        zsplit=(0, 60, 100), n1=200, sita_t=1e-4, sfa1=2.0, sfa2=2.0, T0=1e-3, Tn=10.0, Nt=81,
+        comps=(1, 1, 0, 1, 1, 1),
+        model=dict(kind="marine", water=3.2, sediment=1.0, water_depth=1000.0,
+                   perturb=dict(sigma_log10=0.2, corr=200.0, seed=42),
+                   blocks=[((-2000.0, 2000.0), (-2000.0, 2000.0), (2000.0, 2100.0), 0.01)]),
+        receivers=[(-5000.0 + 500.0 * i, -5000.0 + 500.0 * j, 1000.0) for j in range(21) for i in range(21)],
+        transmitters=[dict(ort=1, len=50.0, x=0.0, y=0.0, z=950.0)],
+    ),
+    # the 3-D marine survey on the same 256 x 256 x 160 grid with 35-cell (not 40-cell) boundary
+    # strips: 187 uniform continuation points per strip instead of 280, below the 256 points
+    # one block of the reference's strip kernels covers (see the oracle's notes on
+    # SplineGridConvIR2R.cu:180-498); 560 x 560 plane
+    "marine3d_strip35_256x256x160": _base(
+        dmin=(25.0, 25.0, 25.0), arg1=1.08, arg2=1.08, xsplit=(0, 35, 186, 35, 0), ysplit=(0, 35, 186),
         zsplit=(0, 60, 100), n1=200, sita_t=1e-4, sfa1=2.0, sfa2=2.0, T0=1e-3, Tn=10.0, Nt=81,
         comps=(1, 1, 0, 1, 1, 1),
         model=dict(kind="marine", water=3.2, sediment=1.0, water_depth=1000.0,
@@ -338,6 +375,33 @@ def batch_case(seed, size=((96, 192), (96, 192), (96, 128)), tn=(1.0,)):
         receivers=[(float(x), 0.0, ztx + dmin) for x in xr],
         transmitters=[dict(ort=1, len=2 * dmin, x=xtx, y=0.0, z=ztx)],
     )
+
+
+def memory_case(c):
+    """The survey of case ``c`` as the (model, survey) values of the in-memory open
+    (api.memory_records / tcsem_open): the same numbers write_case puts in the four files."""
+    g = grid_axes(c)
+    ALx2, ALx1, Nx, ARx1, ARx2 = c["xsplit"]
+    Ay2, Ay1, Ny = c["ysplit"]
+    Az2, Az1, Nz = c["zsplit"]
+    x0, y0, z0 = c.get("origin", (0.0, 0.0, 0.0))
+    model = dict(sfa1=c["sfa1"], sfa2=c["sfa2"], n1=int(c["n1"]), sita_t=c["sita_t"], x0=x0, y0=y0, z0=z0,
+                 dxmin=c["dmin"][0], dymin=c["dmin"][1], dzmin=c["dmin"][2], arg1=c["arg1"], arg2=c["arg2"],
+                 ALx2=ALx2, ALx1=ALx1, Nx=Nx, ARx1=ARx1, ARx2=ARx2, Ay2=Ay2, Ay1=Ay1, Ny=Ny, Az2=Az2, Az1=Az1, Nz=Nz,
+                 con=conductivity(c, g))
+    rx = c["receivers"]
+    tx = []
+    for t in c["transmitters"]:
+        d = dict(ort=int(t["ort"]), len=t["len"], x=t["x"], y=t["y"], z=t["z"],
+                 rx=list(t.get("rx", range(1, len(rx) + 1))))
+        if t["ort"] >= 4:
+            d.update(azi=t["azi"], dip=t["dip"])
+        if t["ort"] == 5:
+            d.update(len1=t["len1"], x1=t["x1"], y1=t["y1"], z1=t["z1"], azi1=t["azi1"], dip1=t["dip1"])
+        tx.append(d)
+    survey = dict(T0=c["T0"], Tn=c["Tn"], Nt=int(c["Nt"]), IsLog=int(c["islog"]), comps=list(c["comps"]),
+                  rx_xyz=np.array(rx, dtype=np.float64), tx=tx)
+    return model, survey
 
 
 def case(name, **overrides):
