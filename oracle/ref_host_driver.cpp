@@ -57,6 +57,14 @@ int main(int argc, char **argv) {
     puti("dims", dims, 17);
     double par[] = {sfa1, sfa2, sita_t, minsita, miu, tRx.T0, tRx.Tn};
     put("params", par, 7);
+    /* the whole ModelPara record, fields in declaration order (FTDT.h:78-110), for drivers of
+     * the reference's device code */
+    int mpi[] = {MP.AnLx_old, MP.AnRx_old, MP.Any_old, MP.Anz, MP.ALx1, MP.ALx2, MP.ARx1, MP.ARx2,
+                 MP.Ay1, MP.Ay2, MP.Az1, MP.Az2, MP.L, MP.M, MP.N, MP.Nx, MP.Ny, MP.Nz,
+                 MP.AnLx_New, MP.AnRx_New, MP.Any_New, MP.LNx2, MP.LMy2};
+    puti("mp_i", mpi, 23);
+    double mpd[] = {MP.dxmin, MP.dymin, MP.dzmin, MP.arg1, MP.arg2};
+    put("mp_d", mpd, 5);
     put("dx", MG.dx, L); put("dy", MG.dy, M); put("dz", MG.dz, N);
     put("X", MG.X_Bzold, L); put("Y", MG.Y_Bzold, M); put("Z", MG.Z, N);
     put("Xn", MG.X_BzNew, L1); put("Yn", MG.Y_BzNew, M1);

@@ -20,7 +20,8 @@ sys.path.insert(0, ROOT)
 from oracle import build_ref  # noqa: E402
 from tcsem_fdtd_gb300 import inputs  # noqa: E402
 
-CASES = ["tiny", "small", "txvar", "example", "halfspace_64x64x48", "marine1d_128x128x96", "marine3d_256x256x160"]
+CASES = ["tiny", "small", "txvar", "example", "halfspace_64x64x48", "marine1d_128x128x96", "marine3d_256x256x160",
+         "wide_142x36x25", "marine3d_strip35_256x256x160"]
 
 
 def read_records(path):

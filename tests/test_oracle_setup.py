@@ -12,7 +12,8 @@ import pytest
 
 from conftest import GOLDEN
 
-CASES = ["tiny", "small", "txvar", "example", "halfspace_64x64x48", "marine1d_128x128x96", "marine3d_256x256x160"]
+CASES = ["tiny", "small", "txvar", "example", "halfspace_64x64x48", "marine1d_128x128x96", "marine3d_256x256x160",
+         "wide_142x36x25", "marine3d_strip35_256x256x160"]
 
 
 def load(name):
