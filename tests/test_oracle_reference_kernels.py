@@ -17,6 +17,16 @@ sampling state machine -- reproduces them (criteria of tests/traces.py, 1e-10 he
 The reference defines only its first transmitter (its counters carry over); the other
 transmitters of txvar and wide_142x36x25 ran with the reference's kernels from a zero state.
 
+On the 256 x 256 x 160 grid the reference's kernels are not deterministic: repeated runs of
+the same survey differ from each other, by up to 1.7e-9 of the largest trace after 800
+steps (three runs of marine3d_strip35_256x256x160 on a GB300); on the smaller grids they
+agree to 4e-15.  Its E and B kernels stage a plane of their inputs in shared memory and
+refill it for the next plane without a barrier after the reads of the previous plane
+(UpdateBx, Bderivate.cu:94-125; UpdateBy; UpdateEy/UpdateEz, ElectricalFiled.cu:178-345):
+a warp that runs ahead overwrites values a neighbouring warp of the block has not read yet.
+The oracle and the product compute each plane from its own values, and are compared with
+that run on the scale of the survey's largest trace.
+
 One reference run is not finite: marine3d_256x256x160, whose 40-cell boundary strips give
 280 uniform continuation points per strip.  The reference's strip kernels
 (Intep_BzIR2R_0x/1x/0y/1y, SplineGridConvIR2R.cu:180-498) run 256 threads per block over a
@@ -38,7 +48,7 @@ from conftest import GOLDEN
 
 sys.path.insert(0, GOLDEN)
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from traces import compare  # noqa: E402
+from traces import compare, field_error  # noqa: E402
 
 
 def ref(case):
@@ -77,8 +87,7 @@ def test_oracle_halfspace_run_matches_the_reference_kernels():
     check(got, z["tx0_traces"], 2, 2e-8)
 
 
-@pytest.mark.parametrize("case", ["marine1d_128x128x96", "marine3d_strip35_256x256x160"])
-def test_oracle_first_400_steps_match_the_reference_kernels(case):
+def first_400_steps(case):
     import gen_oracle_traces as g
 
     z = ref(case)
@@ -88,7 +97,21 @@ def test_oracle_first_400_steps_match_the_reference_kernels(case):
     reached = np.nonzero(np.abs(got).max(axis=(0, 1)))[0]
     k = int(reached[-1])  # samples before the last one the window reached are complete
     assert k >= 10
-    check(got[..., :k], exp[..., :k], 2, 1e-10)
+    return got[..., :k], exp[..., :k]
+
+
+def test_oracle_first_400_steps_match_the_reference_kernels_1d_marine():
+    got, exp = first_400_steps("marine1d_128x128x96")
+    check(got, exp, 2, 1e-10)
+
+
+def test_oracle_first_400_steps_match_the_reference_kernels_3d_marine():
+    """On the 256 x 256 x 160 grid the reference's own runs differ from each other (see the
+    module notes): three runs of 800 steps of marine3d_strip35_256x256x160 spread by up to
+    1.7e-9 of the largest trace, while on 128 x 128 x 96 they agree to 4e-15.  The oracle is
+    compared on that scale: 1e-8 of the largest trace of each field (measured 2.5e-9)."""
+    got, exp = first_400_steps("marine3d_strip35_256x256x160")
+    assert field_error(got, exp, 2) < 1e-8
 
 
 def test_reference_run_with_280_point_strips_is_not_finite():
