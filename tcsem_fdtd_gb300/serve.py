@@ -100,20 +100,25 @@ class Server:
         self.batch.close()
 
 
-def make_stream(n, rate, seed, size=((64, 256), (64, 256), (48, 160)), tn=(1.0, 10.0), root=None):
-    """Seeded Poisson stream of `n` survey requests (mean `rate` per second); writes their inputs."""
+def make_stream(n, rate, seed, size=((64, 256), (64, 256), (48, 160)), tn=(1.0, 10.0), root=None, pool=0):
+    """Seeded Poisson stream of `n` survey requests (mean `rate` per second); writes their inputs.
+    `pool` > 0: the requests draw their surveys (seeded) from that many distinct generated
+    surveys, so a long stream does not need one input directory per request on disk; every
+    request is still a simulation of its own."""
     from .inputs import batch_case, write_case
 
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
     arrivals -= arrivals[0]
     root = root or tempfile.mkdtemp(prefix="tcsem_serve_")
-    reqs = []
-    for r in range(n):
+    ndirs = min(n, pool) if pool > 0 else n
+    dirs = []
+    for r in range(ndirs):
         d = os.path.join(root, f"req{r:04d}")
         write_case(batch_case(int(rng.integers(1 << 31)), size=size, tn=tn), d)
-        reqs.append(Request(r, d, float(arrivals[r])))
-    return reqs
+        dirs.append(d)
+    pick = rng.integers(0, ndirs, size=n) if ndirs < n else np.arange(n)
+    return [Request(r, dirs[int(pick[r])], float(arrivals[r])) for r in range(n)]
 
 
 def request_record(req, mode="batched"):
@@ -181,11 +186,12 @@ def main(argv=None):
     ap.add_argument("--tn", type=float, nargs="+", default=[1.0, 10.0])
     ap.add_argument("--plain", action="store_true", help="also serve the stream one request at a time")
     ap.add_argument("--jsonl", default=None, help="write one JSON line per finished request to this file")
+    ap.add_argument("--pool", type=int, default=0, help="distinct surveys the requests draw from (0: one each)")
     a = ap.parse_args(argv)
     from . import build
 
     build.build()
-    reqs = make_stream(a.requests, a.rate, a.seed, tn=tuple(a.tn))
+    reqs = make_stream(a.requests, a.rate, a.seed, tn=tuple(a.tn), pool=a.pool)
     srv = Server(budget=int(a.budget_gb * (1 << 30)), block=a.block)
     log = open(a.jsonl, "w") if a.jsonl else None
     try:
