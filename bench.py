@@ -159,9 +159,29 @@ def cpu_reference(args, d, cells):
     t0 = time.perf_counter()
     _, ran = orc.run(0, max_steps=n)
     dt = time.perf_counter() - t0
-    return {"value": cells * ran / dt / 1e9, "unit": "Gcell-steps/s", "cores": num_threads(), "kind": "port",
-            "sample": f"{ran} time steps of the {args.workload} workload from a zero state (FP64 C restatement, "
-                      f"{num_threads()} OpenMP threads), {dt:.2f} s"}
+    out = {"value": cells * ran / dt / 1e9, "unit": "Gcell-steps/s", "cores": num_threads(), "kind": "port",
+           "sample": f"{ran} time steps of the {args.workload} workload from a zero state (FP64 C restatement, "
+                     f"{num_threads()} OpenMP threads), {dt:.2f} s"}
+    remap = reference_cpu_remap(d)
+    if remap:
+        out["reference_remap"] = remap
+    return out
+
+
+def reference_cpu_remap(d, reps=20):
+    """The reference's own CPU spline remap (SplineGridConvIR2R_cpu.cpp, built from its tree into
+    oracle/_ref/ref_cpu_remap where the tree is present) timed on this host's cores; None where
+    the binary is absent (it is built for the host it was compiled on)."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_cpu_remap")
+    if not os.access(exe, os.X_OK):
+        return None
+    try:
+        r = subprocess.run([exe, d, str(reps)], capture_output=True, text=True, timeout=120)
+        l1, m1, thr, n, sec, _ = r.stdout.split()
+    except Exception:
+        return None
+    return {"ms_per_call": float(sec) * 1e3, "plane": [int(l1), int(m1)], "cores": int(thr), "kind": "reference",
+            "sample": f"{n} calls of SplineGridConvIR2R_cpu on a seeded top plane of the workload"}
 
 
 def run_reference_arm(args, dist):

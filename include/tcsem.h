@@ -152,7 +152,8 @@ tcsem_status tcsem_synchronize(tcsem_sim_t *sim);
  * of tcsem_advance calls, what the next step needs -- the current fields, their
  * Bz chunk totals, the receiver samples so far and the step -- to `path`;
  * load_state reads it into a handle opened on the same survey with the same
- * precision and z-chunk layout (TCSEM_ERR_INVALID otherwise), after which
+ * precision, z-chunk layout, padded-plane mode and dual-bipole option
+ * (TCSEM_ERR_INVALID otherwise: the run would continue under other physics), after which
  * tcsem_advance continues the run: its traces equal those of the uninterrupted
  * run bit for bit. */
 tcsem_status tcsem_save_state(tcsem_sim_t *sim, const char *path);

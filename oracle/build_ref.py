@@ -7,6 +7,9 @@ TEST INFRASTRUCTURE.  Compiles, from the reference source tree where it lies
   SourceWave.cpp, ModelGridMapping.cpp, LoadRxTxPos.cpp, logspace.cpp,
   AuxiliaryMemory.cpp) linked with oracle/ref_host_driver.cpp; it writes the
   setup arrays the reference computes for a survey directory;
+* oracle/_ref/ref_cpu_remap -- the reference's CPU spline remap
+  (SplineGridConvIR2R_cpu.cpp) with the host setup files and
+  oracle/ref_cpu_remap_driver.cpp, timed as a CPU baseline;
 * oracle/_ref/<name>.cubin -- the reference's device code, unmodified, in its
   default FP64 build, compiled for sm_103a as device-only modules (no host
   code, so they load on any host): ElectricalFiled.cu, Bderivate.cu,
@@ -62,6 +65,29 @@ def build_ref_host(verbose=False):
     return exe
 
 
+def build_ref_cpu_remap(verbose=False):
+    """oracle/_ref/ref_cpu_remap: the reference's CPU spline remap (SplineGridConvIR2R_cpu.cpp,
+    with its host setup files) under oracle/ref_cpu_remap_driver.cpp, for the CPU baseline."""
+    if not reference_present() or not os.path.exists(os.path.join(REF, "SplineGridConvIR2R_cpu.cpp")):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    exe = os.path.join(OUT, "ref_cpu_remap")
+    srcs = [os.path.join(REF, f) for f in HOST_SOURCES + ["SplineGridConvIR2R_cpu.cpp"]] + \
+        [os.path.join(HERE, "ref_cpu_remap_driver.cpp")]
+    if os.path.exists(exe) and all(os.path.getmtime(exe) > os.path.getmtime(s) for s in srcs):
+        return exe
+    cuda_inc = os.path.join(_cuda_home(), "include")
+    # optimised as the reference's Makefile compiles its C++ (-Ofast is -O3 with fast math there;
+    # -O3 here, no -march=native so the binary is the same on every host of this architecture)
+    cmd = ["g++", "-O3", "-fopenmp", "-w", "-Dpow10=exp10", "-include", "cmath", "-include", "limits",
+           "-include", "vector", "-include", "algorithm", "-I", os.path.join(HERE, "shim"), "-I", REF,
+           "-I", cuda_inc, "-o", exe] + srcs
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    return exe
+
+
 def cubin_path(src):
     return os.path.join(OUT, os.path.splitext(src)[0] + ".cubin")
 
@@ -94,4 +120,5 @@ if __name__ == "__main__":
     exe = build_ref_host(verbose=True)
     print(exe or "reference tree absent: nothing built")
     print(build_ref_cubins(verbose=True) or "")
+    print(build_ref_cpu_remap(verbose=True) or "")
     sys.exit(0)

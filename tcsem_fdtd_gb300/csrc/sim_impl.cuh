@@ -974,11 +974,15 @@ template <typename T> struct SimImpl : SimBase {
 
     // ---- checkpoint of a run in progress: what one step hands the next (the field set the
     // next step reads, its Bz chunk totals, the receiver slots and traces so far, the step)
+    // version 2 adds what changes the physics of the continuing run: the continuation plane
+    // (L1 x M1 and the padded-plane mode), the dual-bipole option and the schedule's length
     struct StateHeader {
         char magic[8];
         int version, tsize, L, M, N, itx, cur, nch;
         int kb[kMaxChunks + 1];
         long long step, field_bytes, tot_bytes, ef0_bytes, efs_bytes;
+        int L1, M1, padded_plane, fix_dual_bipole;
+        long long nsteps;
     };
     void save_state(const char *path) override {
         if (!begun) throw Error(TCSEM_ERR_STATE, "tcsem_begin must precede tcsem_save_state");
@@ -986,7 +990,9 @@ template <typename T> struct SimImpl : SimBase {
         check_device_error();
         StateHeader h{};
         std::memcpy(h.magic, "TCSEMST", 8);
-        h.version = 1; h.tsize = (int)sizeof(T); h.L = model.L; h.M = model.M; h.N = model.N;
+        h.version = 2; h.tsize = (int)sizeof(T); h.L = model.L; h.M = model.M; h.N = model.N;
+        h.L1 = model.L1; h.M1 = model.M1; h.padded_plane = opts.padded_plane;
+        h.fix_dual_bipole = opts.fix_dual_bipole != 0; h.nsteps = sched.nsteps;
         h.itx = itx; h.cur = cur; h.nch = zc.n;
         for (int c = 0; c <= kMaxChunks; c++) h.kb[c] = zc.kb[c];
         h.step = step;
@@ -1026,13 +1032,16 @@ template <typename T> struct SimImpl : SimBase {
             std::fclose(f);
             throw Error(st, m);
         };
-        if (!ok || std::memcmp(h.magic, "TCSEMST", 8) != 0 || h.version != 1) fail(TCSEM_ERR_PARSE, std::string(path) + " is not a saved run state");
+        if (!ok || std::memcmp(h.magic, "TCSEMST", 8) != 0 || h.version != 2) fail(TCSEM_ERR_PARSE, std::string(path) + " is not a saved run state");
         bool same = h.tsize == (int)sizeof(T) && h.L == model.L && h.M == model.M && h.N == model.N && h.nch == zc.n &&
                     h.field_bytes == (long long)fld[0][0].n && h.tot_bytes == (long long)zc.n * g.PS * (long long)sizeof(T) &&
                     (h.cur == 0 || h.cur == 1) && h.step >= 0 && h.step <= sched.nsteps && h.itx >= 0 &&
-                    h.itx < (int)model.in.tx.size();
+                    h.itx < (int)model.in.tx.size() && h.L1 == model.L1 && h.M1 == model.M1 &&
+                    h.padded_plane == opts.padded_plane && h.fix_dual_bipole == (opts.fix_dual_bipole != 0) &&
+                    h.nsteps == sched.nsteps;
         for (int c = 0; c <= zc.n && same; c++) same = h.kb[c] == zc.kb[c];
-        const std::string other = std::string(path) + " was saved by a different survey, precision or z-chunk layout";
+        const std::string other = std::string(path) + " was saved by a different survey, precision, z-chunk layout, "
+                                                      "continuation plane or dual-bipole option";
         if (!same) fail(TCSEM_ERR_INVALID, other);
         try {
             begin(h.itx);  // the transmitter's tables (receiver buffers) and a zero state, then the saved arrays
