@@ -143,8 +143,9 @@ def test_cli_usage_error_exit_code():
 
 
 def test_integration_snippets_compile_against_the_header(tmp_path):
-    """The C code INTEGRATION.md gives a maintainer compiles against include/tcsem.h and links
-    against the library's exported symbols (gcc; the snippets placed in a main())."""
+    """The C code of the integration guide at the repository root compiles against
+    include/tcsem.h and links against the library's exported symbols (gcc; the snippets placed
+    in a main())."""
     import re
     import shutil
     import subprocess
@@ -172,7 +173,7 @@ def test_integration_snippets_compile_against_the_header(tmp_path):
 
 
 def test_integration_guide_covers_every_entry_point():
-    """Every function include/tcsem.h declares is described in INTEGRATION.md."""
+    """Every function include/tcsem.h declares is described in the integration guide."""
     from tcsem_fdtd_gb300.api import HEADER, declared_functions
 
     doc = open(os.path.join(os.path.dirname(HEADER), "..", "INTEGRATION.md")).read()

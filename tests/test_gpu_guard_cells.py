@@ -24,6 +24,8 @@ def read_state(path):
     off += (-off) % 8
     step, field_bytes, tot_bytes, ef0_bytes, efs_bytes = np.frombuffer(raw, dtype="<i8", count=5, offset=off)
     off += 5 * 8
+    assert int(ints[0]) == 2  # version 2: L1 M1 padded_plane fix_dual_bipole (int32), nsteps (int64) follow
+    off += 4 * 4 + 8
     assert len(raw) == off + 6 * int(field_bytes) + int(tot_bytes) + int(ef0_bytes) + int(efs_bytes)
     tsize, L, M, N = int(ints[1]), int(ints[2]), int(ints[3]), int(ints[4])
     dt = "<f8" if tsize == 8 else "<f4"
