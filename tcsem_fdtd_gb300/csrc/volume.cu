@@ -272,7 +272,8 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
             t.syk[c] = sy1;
             t.szk[c] = sz1;
         }
-        if (upd && src_tile && s.wave != T(0)) {  // AddTx_*: subtracted after the update of the cell
+        // AddTx_*: subtracted after the update of the cell, on the planes where a segment meets the tile
+        if (upd && src_tile && s.wave != T(0) && k >= t.s_flag[1] && k <= t.s_flag[2]) {
 #pragma unroll
             for (int c = 0; c < NC; c++) {
                 if (!(t.vEx[c] || t.vEy[c])) continue;
@@ -405,10 +406,25 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
         s_z[3 * e + 2] = in ? ax.dzk[k] : T(0);
     }
 
+    bool src_tile = false;  // tile-uniform: does any source segment touch this tile, and on which planes?
+    int sk0 = N, sk1 = -1;
+    for (int q = 0; q < src.nseg; q++) {
+        int a0 = src.i[q], a1 = src.i[q], b0 = src.j[q], b1 = src.j[q], c1 = src.k[q];
+        if (src.comp[q] == 0) a1 += src.count[q] - 1;
+        if (src.comp[q] == 1) b1 += src.count[q] - 1;
+        if (src.comp[q] == 2) c1 += src.count[q] - 1;
+        if (a1 >= t.i0 && a0 <= t.i0 + TX && b1 >= t.j0 && b0 <= t.j0 + BY) {
+            src_tile = true;
+            sk0 = min(sk0, src.k[q]);
+            sk1 = max(sk1, c1);
+        }
+    }
     if (tid == 0) {
         for (int r = 0; r < RING; r++) mbar_init(t.bars + r, 1);
         mbar_init_fence();
-        *t.s_flag = 0;
+        t.s_flag[0] = 0;
+        t.s_flag[1] = sk0;  // read by the source epilogue, after the barrier below
+        t.s_flag[2] = sk1;
     }
     __syncthreads();
     if (tid == 0)  // planes ktop .. ktop-3 into slots 0..3
@@ -465,13 +481,6 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
         t.byk[q] = p0[ABY * BS];
         t.ex1[q] = t.ey1[q] = t.exn[q] = t.eyn[q] = t.ezn[q] = T(0);
         t.bxo1[q] = t.byo1[q] = t.bxn[q] = t.byn[q] = t.acc[q] = T(0);
-    }
-    bool src_tile = false;  // tile-uniform: does any source segment touch this tile?
-    for (int q = 0; q < src.nseg; q++) {
-        int a0 = src.i[q], a1 = src.i[q], b0 = src.j[q], b1 = src.j[q];
-        if (src.comp[q] == 0) a1 += src.count[q] - 1;
-        if (src.comp[q] == 1) b1 += src.count[q] - 1;
-        if (a1 >= t.i0 && a0 <= t.i0 + TX && b1 >= t.j0 && b0 <= t.j0 + BY) src_tile = true;
     }
 
     bool ok = true;
