@@ -191,7 +191,7 @@ template <typename T> struct SweepThread {
     int so[fs3::NC], xo[fs3::NC], i[fs3::NC], col[fs3::NC];
     bool own[fs3::NC], vEx[fs3::NC], vEy[fs3::NC], vEz[fs3::NC];
     T rdx2[fs3::NC], rdx[fs3::NC], fx[fs3::NC];
-    T oc0[fs3::NC], oci[fs3::NC], ocj[fs3::NC], od0[fs3::NC], odi[fs3::NC], odj[fs3::NC];  // Bz chunk offsets
+    T oc0[fs3::NC], oci[fs3::NC], ocj[fs3::NC];  // Bz chunk offsets of the plane being updated: at, left of, below the cell
     T ex1[fs3::NC], ey1[fs3::NC], exn[fs3::NC], eyn[fs3::NC], ezn[fs3::NC];
     T bxo1[fs3::NC], byo1[fs3::NC], bxn[fs3::NC], byn[fs3::NC], acc[fs3::NC];
     T sxk[fs3::NC], syk[fs3::NC], szk[fs3::NC], bxk[fs3::NC], byk[fs3::NC];  // sigma sums and own B of plane k
@@ -242,9 +242,9 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
             const T sx1 = a1 + c1, sy1 = a1 + b1, sz1 = sx1 + b1 + d1;
             const T exo = p0[AEX * BS], eyo = p0[AEY * BS], ezo = p0[AEZ * BS];
             if (upd) {
-                const T bz = p0[ABZ * BS] + (lo ? t.oc0[c] : t.od0[c]);
-                const T bzi = p0[ABZ * BS - 1] + (lo ? t.oci[c] : t.odi[c]);
-                const T bzj = p0[ABZ * BS - BXW] + (lo ? t.ocj[c] : t.odj[c]);
+                const T bz = p0[ABZ * BS] + t.oc0[c];
+                const T bzi = p0[ABZ * BS - 1] + t.oci[c];
+                const T bzj = p0[ABZ * BS - BXW] + t.ocj[c];
                 const T byi = p0[ABY * BS - 1], bxj = p0[ABX * BS - BXW];
                 // DuFort-Frankel update (ElectricalFiled.cu:89-345) of the three components, computed for
                 // every cell and kept where the component is updated; s.dt carries the 1/4 of the sigma sums
@@ -336,6 +336,16 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
         }
     }
     return true;
+}
+
+// the cells' Bz chunk offsets from one of the two offset boxes
+template <typename T> __device__ __forceinline__ void set_offsets(SweepThread<T> &t, const T *box) {
+#pragma unroll
+    for (int q = 0; q < fs3::NC; q++) {
+        t.oc0[q] = box[t.so[q]];
+        t.oci[q] = box[t.so[q] - 1];
+        t.ocj[q] = box[t.so[q] - fs3::BXW];
+    }
 }
 
 // one CTA of the sweep: tile (bx, by) of z-chunk c with the step scalars s
@@ -470,8 +480,6 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
 #pragma unroll
     for (int q = 0; q < NC; q++) {
         const int so = t.so[q];
-        t.oc0[q] = s_oc[so]; t.oci[q] = s_oc[so - 1]; t.ocj[q] = s_oc[so - BXW];
-        t.od0[q] = s_oc1[so]; t.odi[q] = s_oc1[so - 1]; t.odj[q] = s_oc1[so - BXW];
         const T *p0 = t.ring + so;  // carried values of plane ktop (slot 0)
         const T a = p0[ASG * BS], b = p0[ASG * BS - 1], cc = p0[ASG * BS - BXW], d = p0[ASG * BS - BXW - 1];
         t.sxk[q] = a + cc;
@@ -483,10 +491,14 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
         t.bxo1[q] = t.byo1[q] = t.bxn[q] = t.byn[q] = t.acc[q] = T(0);
     }
 
+    // Bz offsets of the first plane: ktop is the halo plane k1 of the chunk below (its offsets) or the
+    // zero bottom; every later plane lies in this chunk
+    set_offsets(t, ktop < N ? s_oc1 : s_oc);
     bool ok = true;
     unsigned rp = 0;  // parity of the ring round
     for (int k = ktop; ok && k >= t.k0 - 1; k -= RING, rp ^= 1u) {
         ok = sweep_plane<T, 0>(t, k, rp, s, s_z, out, src, src_tile);
+        if (k == ktop) set_offsets(t, s_oc);
         if (!ok || k - 1 < t.k0 - 1) break;
         ok = sweep_plane<T, 1>(t, k - 1, rp, s, s_z, out, src, src_tile);
         if (!ok || k - 2 < t.k0 - 1) break;
