@@ -174,6 +174,21 @@ template <> __device__ __forceinline__ float rcp_fast<float>(float x) {
 }
 template <> __device__ __forceinline__ double rcp_fast<double>(double x) { return 1.0 / x; }
 
+// the three reciprocals of the E update: three MUFU ops in FP32; in FP64, where a division
+// costs about ten FP64 pipe operations and the pipe bounds the sweep, one division of the
+// product and five multiplies (1/a = bc / abc, ...), a few ulp from three divisions
+__device__ __forceinline__ void recip3(float a, float b, float c, float &ra, float &rb, float &rc) {
+    ra = rcp_fast(a);
+    rb = rcp_fast(b);
+    rc = rcp_fast(c);
+}
+__device__ __forceinline__ void recip3(double a, double b, double c, double &ra, double &rb, double &rc) {
+    const double ab = a * b, r = 1.0 / (ab * c), rab = c * r;
+    rc = ab * r;
+    ra = b * rab;
+    rb = a * rab;
+}
+
 // per-thread state of the sweep (NC cells per thread); sweep_plane<PH>() advances
 // one z-plane with PH = (ktop - k) mod 4, so ring slots and exchange parities
 // are compile-time constants
@@ -249,7 +264,8 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
                 // DuFort-Frankel update (ElectricalFiled.cu:89-345) of the three components, computed for
                 // every cell and kept where the component is updated; s.dt carries the 1/4 of the sigma sums
                 const T sdx = (t.sxk[c] + sx1) * s.dt, sdy = (t.syk[c] + sy1) * s.dt, sdz = t.szk[c] * s.dt;
-                const T rx = rcp_fast(s.lam2 + sdx), ry = rcp_fast(s.lam2 + sdy), rz = rcp_fast(s.lam2 + sdz);
+                T rx, ry, rz;
+                recip3(s.lam2 + sdx, s.lam2 + sdy, s.lam2 + sdz, rx, ry, rz);
                 const T cx = (bz - bzj) * t.rdy2 - (t.byk[c] - bym) * rzs;
                 const T cy = (t.bxk[c] - bxm) * rzs - (bz - bzi) * t.rdx2[c];
                 const T cz = (t.byk[c] - byi) * t.rdx2[c] - (t.bxk[c] - bxj) * t.rdy2;
