@@ -34,6 +34,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+// Programmatic dependent launch: let the next kernel on the stream start (its blocks become
+// resident and run up to their wait), and wait for the previous kernel's completion and memory.
+// Without the launch attribute on the dependent kernel both are no-ops.
+__device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait_prev() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // 3-D tiled tensor copy global -> shared, completing on bar
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
     asm volatile(

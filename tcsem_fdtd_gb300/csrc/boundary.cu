@@ -34,8 +34,6 @@ constexpr int kBndThreads = 256;
 // it reads what this grid wrote.  Without the launch attribute the wait returns at once.
 // Releasing the next kernel only at the end keeps its waiting blocks from holding SM
 // resources that the sweep running beside the boundary needs.
-__device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait_prev() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // Natural-spline second derivatives mb[0..n) of the line y[0..n) (stride ys) from
 // the precomputed elimination factors tab = g | w | inv | du (n values each): the
@@ -405,7 +403,8 @@ __device__ __forceinline__ void bilinear_cta(const BoundaryDev<T> &bd, T *bx, T 
     const int L = g.L, M = g.M;
     const int nbx = (L + 1) * M, nby = L * (M + 1);
     const T norm = bd.inv_norm;
-    pdl_wait_prev();  // Z is the previous kernel's output
+    pdl_allow_next();  // the top z-chunk of the sweep may stage its planes; it waits for this grid before the air plane
+    pdl_wait_prev();   // Z is the previous kernel's output
     for (int e = blk * blockDim.x + threadIdx.x; e < nbx + nby; e += nblk * blockDim.x) {
         if (e < nbx) {
             const int j = e / (L + 1), i = e % (L + 1);

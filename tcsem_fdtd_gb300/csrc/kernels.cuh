@@ -105,12 +105,13 @@ struct SweepMaps {
 };
 // chunks c0 .. c1-1 in one launch; rev = the last chunk's blocks first (consecutive
 // steps alternate, so a step starts on the planes the previous one wrote last,
-// which may still be in L2)
+// which may still be in L2); pdl = programmatic dependent launch after the previous
+// kernel on the stream (the CTAs wait for it before loading the air plane k = -1)
 template <typename T>
 void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
                         const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
                         const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, bool rev, int *err,
-                        cudaStream_t st);
+                        cudaStream_t st, bool pdl = false);
 template <typename T> cudaError_t sweep_configure(int N);
 template <typename T> size_t sweep_smem_bytes(int N);
 template <typename T> int sweep_blocks_per_sm(int N);  // resident sweep CTAs per SM (after sweep_configure)

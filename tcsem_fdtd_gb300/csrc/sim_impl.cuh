@@ -471,7 +471,7 @@ template <typename T> struct SimImpl : SimBase {
         }
     }
     void sweep(int b, StepScalars<T> s, const StepScalars<T> *table, StepGate gate, int c0 = 0, int c1 = -1,
-               cudaStream_t st = nullptr) {
+               cudaStream_t st = nullptr, bool pdl = false) {
         if (c1 < 0) c1 = zc.n;
         // Block order: consecutive steps alternate the chunk order (a step starts on the planes
         // the previous one wrote last), except in a launch that includes a top chunk shorter than
@@ -480,7 +480,7 @@ template <typename T> struct SimImpl : SimBase {
         // 256 x 256 x 160 sweep against 121.8 alternating and 125.4 with the top chunk first)
         const bool short_top = c0 == 0 && c1 - c0 > 1 && zc.kb[1] - zc.kb[0] < zc.kb[2] - zc.kb[1];
         launch_fused_sweep<T>(maps[b], g, fs(b ^ 1), tot[b].as<T>(), tot[b ^ 1].as<T>(), ax, s, table, gate, src, zc,
-                              c0, c1, short_top || (b & 1) != 0, errw.as<int>(), st ? st : stream);
+                              c0, c1, short_top || (b & 1) != 0, errw.as<int>(), st ? st : stream, pdl);
     }
     void consolidate(int b) { launch_bz_consolidate<T>(g, fs(b).bz, tot[b].as<T>(), zc, stream); }
 
@@ -768,9 +768,11 @@ template <typename T> struct SimImpl : SimBase {
         if (overlap) {  // fork: boundary -> top chunk on `side`, chunks 1.. on `stream`; receivers on `rxs`
             CK(cudaEventRecord(ev_fork, stream));
             CK(cudaStreamWaitEvent(side, ev_fork, 0));
-            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, side, overlap_pdl);
             CK(cudaStreamWaitEvent(side, ev_rx[b ^ 1], 0));  // set b^1 no longer read by older receivers
-            sweep(b, StepScalars<T>{}, table, gate, 0, 1, side);
+            launch_boundary<T>(bd, g, in.bz, tot[b].as<T>(), zc.n, in.bx, in.by, gate, side, overlap_pdl);
+            // the top chunk directly after the boundary's last stage, launched early: it stages its planes
+            // while the bilinear remap runs and waits for it only before the air plane
+            sweep(b, StepScalars<T>{}, table, gate, 0, 1, side, true);
             CK(cudaStreamWaitEvent(stream, ev_rx[b ^ 1], 0));
             sweep(b, StepScalars<T>{}, table, gate, 1, zc.n, stream);
             CK(cudaEventRecord(ev_join, side));

@@ -335,6 +335,7 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
     }
     // plane k is no longer read: its ring slot takes plane k-4
     if (t.tid == 0 && k - RING >= t.klow && k >= t.k0) {
+        if (k - RING < 0) pdl_wait_prev();  // the air plane is the boundary's output (no-op without the launch attribute)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         uint64_t *b = t.bars + S0;
         mbar_expect_tx(b, t.plane_bytes);
@@ -455,6 +456,9 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
     __syncthreads();
     if (tid == 0)  // planes ktop .. ktop-3 into slots 0..3
         for (int p = ktop, q = 0; q < RING && p >= klow; p--, q++) {
+            // the air plane (k = -1) is the boundary's output: a top chunk launched early (programmatic
+            // dependent launch after the boundary's last stage) stages its other planes first
+            if (p < 0) pdl_wait_prev();
             uint64_t *b = t.bars + q;
             mbar_expect_tx(b, t.plane_bytes);
             for (int a = 0; a < NARR; a++) tma_load_3d(t.ring + (q * NARR + a) * BS, t.maps + a, t.i0, t.j0, p + 1, b);
@@ -565,10 +569,18 @@ template <typename T>
 void launch_fused_sweep(const SweepMaps &maps, const Geom &g, FieldSet<T> out, const T *tin, T *tout,
                         const Axis<T> &ax, StepScalars<T> s, const StepScalars<T> *table, StepGate gate,
                         const SourceTable<T> &src, const ZChunks &zc, int c0, int c1, bool rev, int *err,
-                        cudaStream_t st) {
-    dim3 grd((g.L + fs3::TX - 1) / fs3::TX, (g.M + fs3::BY - 1) / fs3::BY, c1 - c0);
-    k_sweep<T><<<grd, fs3::NT, fs3::smem_bytes_n<T>(g.N), st>>>(maps, g, out, tin, tout, ax, s, table, gate, src, zc,
-                                                                c0, rev ? 1 : 0, err);
+                        cudaStream_t st, bool pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((g.L + fs3::TX - 1) / fs3::TX, (g.M + fs3::BY - 1) / fs3::BY, c1 - c0);
+    cfg.blockDim = dim3(fs3::NT);
+    cfg.dynamicSmemBytes = fs3::smem_bytes_n<T>(g.N);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_sweep<T>, maps, g, out, tin, tout, ax, s, table, gate, src, zc, c0, rev ? 1 : 0, err);
 }
 
 template <typename T>
@@ -622,7 +634,8 @@ template <typename T> void launch_bz_consolidate(const Geom &g, T *bz, T *tot, c
     template void launch_bderivate<T>(const Geom &, FieldSet<T>, const Axis<T> &, T, int *, cudaStream_t);         \
     template void launch_fused_sweep<T>(const SweepMaps &, const Geom &, FieldSet<T>, const T *, T *,             \
                                         const Axis<T> &, StepScalars<T>, const StepScalars<T> *, StepGate,         \
-                                        const SourceTable<T> &, const ZChunks &, int, int, bool, int *, cudaStream_t);       \
+                                        const SourceTable<T> &, const ZChunks &, int, int, bool, int *, cudaStream_t,  \
+                                        bool);                                                                     \
     template cudaError_t sweep_configure<T>(int);                                                                  \
     template size_t sweep_smem_bytes<T>(int);                                                                      \
     template int sweep_blocks_per_sm<T>(int);                                                                      \
