@@ -269,9 +269,22 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
                 const T cx = (bz - bzj) * t.rdy2 - (t.byk[c] - bym) * rzs;
                 const T cy = (t.bxk[c] - bxm) * rzs - (bz - bzi) * t.rdx2[c];
                 const T cz = (t.byk[c] - byi) * t.rdx2[c] - (t.bxk[c] - bxj) * t.rdy2;
-                const T ex = ((s.lam2 - sdx) * rx) * exo + (s.c4 * rx) * cx;
-                const T ey = ((s.lam2 - sdy) * ry) * eyo + (s.c4 * ry) * cy;
-                const T ez = ((s.lam2 - sdz) * rz) * ezo + (s.c4 * rz) * cz;
+                T ex, ey, ez;
+                if constexpr (sizeof(T) == 8) {
+                    // FP64, bound by the FP64 pipe: with D = lam2 + sigma dt, the update
+                    // (lam2 - sigma dt)/D E + c4/D curl is written (2 lam2 E + c4 curl)/D - E -- three
+                    // operations per component after 1/D instead of five.  (In FP32, where 1/D is an
+                    // approximate reciprocal, the same form raised the trace error of a long whole run on
+                    // 142 x 36 x 25 cells to 1.02 % of its peak, and saved 0.3 % of the step time.)
+                    const T l2 = s.lam2 + s.lam2;
+                    ex = fma(fma(s.c4, cx, l2 * exo), rx, -exo);
+                    ey = fma(fma(s.c4, cy, l2 * eyo), ry, -eyo);
+                    ez = fma(fma(s.c4, cz, l2 * ezo), rz, -ezo);
+                } else {
+                    ex = ((s.lam2 - sdx) * rx) * exo + (s.c4 * rx) * cx;
+                    ey = ((s.lam2 - sdy) * ry) * eyo + (s.c4 * ry) * cy;
+                    ez = ((s.lam2 - sdz) * rz) * ezo + (s.c4 * rz) * cz;
+                }
                 t.exn[c] = t.vEx[c] ? ex : exo;
                 t.eyn[c] = t.vEy[c] ? ey : eyo;
                 t.ezn[c] = t.vEz[c] ? ez : ezo;
