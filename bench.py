@@ -163,8 +163,9 @@ def cpu_reference(args, d, cells):
            "sample": f"{ran} time steps of the {args.workload} workload from a zero state (FP64 C restatement, "
                      f"{num_threads()} OpenMP threads), {dt:.2f} s"}
     remap = reference_cpu_remap(d)
-    if remap:
-        out["reference_remap"] = remap
+    out["reference_remap"] = remap or {
+        "unavailable": "the reference's CPU spline remap (SplineGridConvIR2R_cpu.cpp) is built from the reference's "
+                       "sources by oracle/build_ref.py, and this host has neither the sources nor a binary built for it"}
     return out
 
 
