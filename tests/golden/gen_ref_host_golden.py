@@ -3,8 +3,8 @@
 Runs oracle/_ref/ref_host (built by oracle/build_ref.py from the reference's
 ModelingSetup.cpp, SourceWave.cpp, ModelGridMapping.cpp, LoadRxTxPos.cpp,
 logspace.cpp and AuxiliaryMemory.cpp) on the seeded inputs of each case and
-stores every array it reports.  Needs the reference source tree; the GPU machine
-uses the committed .npz files.
+stores every array it reports.  Needs the reference source tree; hosts without it
+use the committed .npz files.
 
     python tests/golden/gen_ref_host_golden.py
 """
