@@ -199,6 +199,7 @@ template <typename T> struct SweepThread {
     const CUtensorMap *maps;
     unsigned plane_bytes;
     int j, PS, N, k0, k1, klow, ktop, tid, i0, j0;
+    int role;  // 0: a row of the tile, 1: the +y halo row, 2: the +x halo column (warp-uniform; FP64)
     int total;  // elements of each field array (bounds-checked builds)
     int *err;
     T rdy2, rdy, fy;  // per row: 1/(dy[j-1]+dy[j]), 1/dy[j], dtb/dy[j]
@@ -212,7 +213,7 @@ template <typename T> struct SweepThread {
     T sxk[fs3::NC], syk[fs3::NC], szk[fs3::NC], bxk[fs3::NC], byk[fs3::NC];  // sigma sums and own B of plane k
 };
 
-template <typename T, int PH>
+template <typename T, int PH, int ROLE>
 __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned rp, const StepScalars<T> &s,
                                             const T *__restrict__ zt, const FieldSet<T> &out,
                                             const SourceTable<T> &src, bool src_tile) {
@@ -222,18 +223,28 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
     constexpr int QE = PH & 1, QB = (PH + 1) & 1;
     constexpr int XP2 = XR * XC;
     const int zi = k - t.klow;  // z tables: rdz, rdzs, dzk of plane klow + zi
+    // Roles (one compiled copy each, FP64 only): the row warps update and store every component; the
+    // +y halo row warp only produces what the tile's last row reads from it (Ex and Ez for By there,
+    // By for Bz), the +x halo column warp what the tile's last column reads (Ey and Ez for Bx there,
+    // Bx for Bz).  Every copy passes the one barrier per plane in the same order.
+    constexpr bool rX = ROLE != 2, rY = ROLE != 1, rR = ROLE == 0;
     // ---- B_new(k+1) from E_new(k+1) (own + neighbours) and E_new(k+2)
     const bool doB = k + 1 < t.k1;
     if (doB) {
         const T fz = zt[3 * (zi + 1)] * s.dtb;  // dtb / dz(k+1)
 #pragma unroll
         for (int c = 0; c < NC; c++) {
-            const T ezj = t.x_ez[QB * XP2 + t.xo[c] + XC], ezi = t.x_ez[QB * XP2 + t.xo[c] + 1];
-            const T bx = t.bxo1[c] + (t.ey1[c] - t.eyn[c]) * fz - (ezj - t.ezn[c]) * t.fy;
-            const T by = t.byo1[c] + (ezi - t.ezn[c]) * t.fx[c] - (t.ex1[c] - t.exn[c]) * fz;
-            t.bxn[c] = t.vEy[c] ? bx : t.bxo1[c];
-            t.byn[c] = t.vEx[c] ? by : t.byo1[c];
-            if (t.own[c] && TCSEM_IN(t.col[c] + (k + 2) * t.PS, t.total, t.err)) {
+            if constexpr (rY) {
+                const T ezj = t.x_ez[QB * XP2 + t.xo[c] + XC];
+                const T bx = t.bxo1[c] + (t.ey1[c] - t.eyn[c]) * fz - (ezj - t.ezn[c]) * t.fy;
+                t.bxn[c] = t.vEy[c] ? bx : t.bxo1[c];
+            }
+            if constexpr (rX) {
+                const T ezi = t.x_ez[QB * XP2 + t.xo[c] + 1];
+                const T by = t.byo1[c] + (ezi - t.ezn[c]) * t.fx[c] - (t.ex1[c] - t.exn[c]) * fz;
+                t.byn[c] = t.vEx[c] ? by : t.byo1[c];
+            }
+            if (rR && t.own[c] && TCSEM_IN(t.col[c] + (k + 2) * t.PS, t.total, t.err)) {
                 const int o = t.col[c] + (k + 2) * t.PS;
                 out.bx[o] = t.bxn[c];
                 out.by[o] = t.byn[c];
@@ -255,39 +266,59 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
             const T a1 = p1[ASG * BS], b1 = p1[ASG * BS - 1], c1 = p1[ASG * BS - BXW], d1 = p1[ASG * BS - BXW - 1];
             const T bym = p1[ABY * BS], bxm = p1[ABX * BS];
             const T sx1 = a1 + c1, sy1 = a1 + b1, sz1 = sx1 + b1 + d1;
-            const T exo = p0[AEX * BS], eyo = p0[AEY * BS], ezo = p0[AEZ * BS];
+            const T ezo = p0[AEZ * BS];
+            T exo = T(0), eyo = T(0);
+            if constexpr (rX) exo = p0[AEX * BS];
+            if constexpr (rY) eyo = p0[AEY * BS];
             if (upd) {
                 const T bz = p0[ABZ * BS] + t.oc0[c];
-                const T bzi = p0[ABZ * BS - 1] + t.oci[c];
-                const T bzj = p0[ABZ * BS - BXW] + t.ocj[c];
                 const T byi = p0[ABY * BS - 1], bxj = p0[ABX * BS - BXW];
                 // DuFort-Frankel update (ElectricalFiled.cu:89-345) of the three components, computed for
                 // every cell and kept where the component is updated; s.dt carries the 1/4 of the sigma sums
                 const T sdx = (t.sxk[c] + sx1) * s.dt, sdy = (t.syk[c] + sy1) * s.dt, sdz = t.szk[c] * s.dt;
-                T rx, ry, rz;
-                recip3(s.lam2 + sdx, s.lam2 + sdy, s.lam2 + sdz, rx, ry, rz);
-                const T cx = (bz - bzj) * t.rdy2 - (t.byk[c] - bym) * rzs;
-                const T cy = (t.bxk[c] - bxm) * rzs - (bz - bzi) * t.rdx2[c];
                 const T cz = (t.byk[c] - byi) * t.rdx2[c] - (t.bxk[c] - bxj) * t.rdy2;
-                T ex, ey, ez;
                 if constexpr (sizeof(T) == 8) {
                     // FP64, bound by the FP64 pipe: with D = lam2 + sigma dt, the update
                     // (lam2 - sigma dt)/D E + c4/D curl is written (2 lam2 E + c4 curl)/D - E -- three
                     // operations per component after 1/D instead of five.  (In FP32, where 1/D is an
                     // approximate reciprocal, the same form raised the trace error of a long whole run on
                     // 142 x 36 x 25 cells to 1.02 % of its peak, and saved 0.3 % of the step time.)
+                    T rx, ry, rz;
+                    recip3(s.lam2 + sdx, s.lam2 + sdy, s.lam2 + sdz, rx, ry, rz);
                     const T l2 = s.lam2 + s.lam2;
-                    ex = fma(fma(s.c4, cx, l2 * exo), rx, -exo);
-                    ey = fma(fma(s.c4, cy, l2 * eyo), ry, -eyo);
-                    ez = fma(fma(s.c4, cz, l2 * ezo), rz, -ezo);
+                    if constexpr (rX) {
+                        const T bzj = p0[ABZ * BS - BXW] + t.ocj[c];
+                        const T cx = (bz - bzj) * t.rdy2 - (t.byk[c] - bym) * rzs;
+                        const T ex = fma(fma(s.c4, cx, l2 * exo), rx, -exo);
+                        t.exn[c] = t.vEx[c] ? ex : exo;
+                    }
+                    if constexpr (rY) {
+                        const T bzi = p0[ABZ * BS - 1] + t.oci[c];
+                        const T cy = (t.bxk[c] - bxm) * rzs - (bz - bzi) * t.rdx2[c];
+                        const T ey = fma(fma(s.c4, cy, l2 * eyo), ry, -eyo);
+                        t.eyn[c] = t.vEy[c] ? ey : eyo;
+                    }
+                    const T ez = fma(fma(s.c4, cz, l2 * ezo), rz, -ezo);
+                    t.ezn[c] = t.vEz[c] ? ez : ezo;
                 } else {
-                    ex = ((s.lam2 - sdx) * rx) * exo + (s.c4 * rx) * cx;
-                    ey = ((s.lam2 - sdy) * ry) * eyo + (s.c4 * ry) * cy;
-                    ez = ((s.lam2 - sdz) * rz) * ezo + (s.c4 * rz) * cz;
+                    if constexpr (rX) {
+                        const T bzj = p0[ABZ * BS - BXW] + t.ocj[c];
+                        const T cx = (bz - bzj) * t.rdy2 - (t.byk[c] - bym) * rzs;
+                        const T rx = rcp_fast(s.lam2 + sdx);
+                        const T ex = ((s.lam2 - sdx) * rx) * exo + (s.c4 * rx) * cx;
+                        t.exn[c] = t.vEx[c] ? ex : exo;
+                    }
+                    if constexpr (rY) {
+                        const T bzi = p0[ABZ * BS - 1] + t.oci[c];
+                        const T cy = (t.bxk[c] - bxm) * rzs - (bz - bzi) * t.rdx2[c];
+                        const T ry = rcp_fast(s.lam2 + sdy);
+                        const T ey = ((s.lam2 - sdy) * ry) * eyo + (s.c4 * ry) * cy;
+                        t.eyn[c] = t.vEy[c] ? ey : eyo;
+                    }
+                    const T rz = rcp_fast(s.lam2 + sdz);
+                    const T ez = ((s.lam2 - sdz) * rz) * ezo + (s.c4 * rz) * cz;
+                    t.ezn[c] = t.vEz[c] ? ez : ezo;
                 }
-                t.exn[c] = t.vEx[c] ? ex : exo;
-                t.eyn[c] = t.vEy[c] ? ey : eyo;
-                t.ezn[c] = t.vEz[c] ? ez : ezo;
             } else {
                 t.exn[c] = exo;
                 t.eyn[c] = eyo;
@@ -320,7 +351,7 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
         }
 #pragma unroll
         for (int c = 0; c < NC; c++) {
-            if (upd && lo && t.own[c] && TCSEM_IN(t.col[c] + (k + 1) * t.PS, t.total, t.err)) {
+            if (rR && upd && lo && t.own[c] && TCSEM_IN(t.col[c] + (k + 1) * t.PS, t.total, t.err)) {
                 const int o = t.col[c] + (k + 1) * t.PS;
                 out.ex[o] = t.exn[c];
                 out.ey[o] = t.eyn[c];
@@ -329,11 +360,11 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
             t.x_ez[QE * XP2 + t.xo[c]] = t.ezn[c];  // publish Ez_new(k)
         }
     }
-    if (doB) {  // publish B_new(k+1)
+    if (doB) {  // publish B_new(k+1): Bx where Bz reads it (rows, +x column), By likewise (rows, +y row)
 #pragma unroll
         for (int c = 0; c < NC; c++) {
-            t.x_bxn[QB * XP2 + t.xo[c]] = t.bxn[c];
-            t.x_byn[QB * XP2 + t.xo[c]] = t.byn[c];
+            if constexpr (rY) t.x_bxn[QB * XP2 + t.xo[c]] = t.bxn[c];
+            if constexpr (rX) t.x_byn[QB * XP2 + t.xo[c]] = t.byn[c];
         }
     }
     // plane k-2 is read by the next plane
@@ -355,8 +386,8 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
 #pragma unroll
         for (int a = 0; a < NARR; a++) tma_load_3d(t.ring + (S0 * NARR + a) * BS, t.maps + a, t.i0, t.j0, k - RING + 1, b);
     }
-    // ---- Bz(k+1) = Bz(k+2) + dz (dBx/dx + dBy/dy)
-    if (doB) {
+    // ---- Bz(k+1) = Bz(k+2) + dz (dBx/dx + dBy/dy), for the tile's own rows
+    if (doB && rR) {
         const T dz = zt[3 * (zi + 1) + 2];
 #pragma unroll
         for (int c = 0; c < NC; c++) {
@@ -368,6 +399,12 @@ __device__ __forceinline__ bool sweep_plane(SweepThread<T> &t, int k, unsigned r
     return true;
 }
 
+// the z-march of one warp through the chunk, in the copy of the plane code for its role
+template <typename T, int ROLE>
+__device__ __forceinline__ bool sweep_march(SweepThread<T> &t, const StepScalars<T> &s, const T *__restrict__ s_z,
+                                            const FieldSet<T> &out, const SourceTable<T> &src, bool src_tile,
+                                            const T *s_oc);
+
 // the cells' Bz chunk offsets from one of the two offset boxes
 template <typename T> __device__ __forceinline__ void set_offsets(SweepThread<T> &t, const T *box) {
 #pragma unroll
@@ -376,6 +413,27 @@ template <typename T> __device__ __forceinline__ void set_offsets(SweepThread<T>
         t.oci[q] = box[t.so[q] - 1];
         t.ocj[q] = box[t.so[q] - fs3::BXW];
     }
+}
+
+template <typename T, int ROLE>
+__device__ __forceinline__ bool sweep_march(SweepThread<T> &t, const StepScalars<T> &s, const T *__restrict__ s_z,
+                                            const FieldSet<T> &out, const SourceTable<T> &src, bool src_tile,
+                                            const T *s_oc) {
+    using namespace fs3;
+    bool ok = true;
+    unsigned rp = 0;  // parity of the ring round
+    const int ktop = t.ktop;
+    for (int k = ktop; ok && k >= t.k0 - 1; k -= RING, rp ^= 1u) {
+        ok = sweep_plane<T, 0, ROLE>(t, k, rp, s, s_z, out, src, src_tile);
+        if (k == ktop) set_offsets(t, s_oc);
+        if (!ok || k - 1 < t.k0 - 1) break;
+        ok = sweep_plane<T, 1, ROLE>(t, k - 1, rp, s, s_z, out, src, src_tile);
+        if (!ok || k - 2 < t.k0 - 1) break;
+        ok = sweep_plane<T, 2, ROLE>(t, k - 2, rp, s, s_z, out, src, src_tile);
+        if (!ok || k - 3 < t.k0 - 1) break;
+        ok = sweep_plane<T, 3, ROLE>(t, k - 3, rp, s, s_z, out, src, src_tile);
+    }
+    return ok;
 }
 
 // one CTA of the sweep: tile (bx, by) of z-chunk c with the step scalars s
@@ -411,6 +469,7 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
     t.k0 = zc.plane(c);
     t.k1 = zc.plane(c + 1);
     const int ty = w < 9 ? w : lane;
+    t.role = w < 8 ? 0 : (w == 8 ? 1 : 2);
     t.j = t.j0 + ty;
     const bool rowok = w < 9 || lane <= BY;
     t.rdy2 = (rowok && t.j >= 1 && t.j < M) ? ax.rdy2[t.j] : T(0);
@@ -527,18 +586,16 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
     // Bz offsets of the first plane: ktop is the halo plane k1 of the chunk below (its offsets) or the
     // zero bottom; every later plane lies in this chunk
     set_offsets(t, ktop < N ? s_oc1 : s_oc);
-    bool ok = true;
-    unsigned rp = 0;  // parity of the ring round
-    for (int k = ktop; ok && k >= t.k0 - 1; k -= RING, rp ^= 1u) {
-        ok = sweep_plane<T, 0>(t, k, rp, s, s_z, out, src, src_tile);
-        if (k == ktop) set_offsets(t, s_oc);
-        if (!ok || k - 1 < t.k0 - 1) break;
-        ok = sweep_plane<T, 1>(t, k - 1, rp, s, s_z, out, src, src_tile);
-        if (!ok || k - 2 < t.k0 - 1) break;
-        ok = sweep_plane<T, 2>(t, k - 2, rp, s, s_z, out, src, src_tile);
-        if (!ok || k - 3 < t.k0 - 1) break;
-        ok = sweep_plane<T, 3>(t, k - 3, rp, s, s_z, out, src, src_tile);
-    }
+    // FP64 (bound by the FP64 pipe): the halo warps run their reduced copies of the plane code
+    // (5 % faster).  FP32 runs one copy in every warp: three copies of its issue-bound loop made the
+    // sweep 40 % slower (measured; presumably the larger loop no longer fits the instruction cache).
+    bool ok;
+    if constexpr (sizeof(T) == 8)
+        ok = t.role == 0 ? sweep_march<T, 0>(t, s, s_z, out, src, src_tile, s_oc)
+             : t.role == 1 ? sweep_march<T, 1>(t, s, s_z, out, src, src_tile, s_oc)
+                           : sweep_march<T, 2>(t, s, s_z, out, src, src_tile, s_oc);
+    else
+        ok = sweep_march<T, 0>(t, s, s_z, out, src, src_tile, s_oc);
     if (!ok) {  // a copy did not arrive (the copies in flight were drained in sweep_plane)
         if (tid == 0) atomicExch(err, 1);
         return;
