@@ -567,10 +567,13 @@ template <typename T>
 void launch_boundary(const BoundaryDev<T> &bd, const Geom &g, const T *bz, const T *tot, int nch, T *bx, T *by,
                      StepGate gate, cudaStream_t st, bool pdl) {
     k_rows_fwd<T><<<(g.M + 1) / 2, kBndThreads, smem_rows(bd, g.L), st>>>(bd, bz, tot, nch, g, gate);
+    // The column stage starts early only where the caller asks (beside a long sweep its early CTAs
+    // would take slots the sweep's single wave needs at the start of a step); the last two stages
+    // always do: by then the sweep's CTAs are all resident.
     launch_after(pdl, k_cols<T>, bd.H, kBndThreads, smem_cols(bd), st, bd, gate);
-    launch_after(pdl, k_rows_inv<T>, bd.S, kBndThreads, smem_inv(bd), st, bd, gate);
+    launch_after(true, k_rows_inv<T>, bd.S, kBndThreads, smem_inv(bd), st, bd, gate);
     int n = (g.L + 1) * g.M + g.L * (g.M + 1);
-    launch_after(pdl, k_bilinear<T>, (n + 255) / 256, 256, (size_t)0, st, bd, bx, by, g, gate);
+    launch_after(true, k_bilinear<T>, (n + 255) / 256, 256, (size_t)0, st, bd, bx, by, g, gate);
 }
 
 #define INST(T)                                                                                            \
