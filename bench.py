@@ -210,7 +210,9 @@ def run_reference_arm(args, dist):
             "warmup": min(args.warmup, 3), "ms_per_step": dt * 1e3 / ran, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": args.workload, "grid": [g["L"], g["M"], g["N"]], "cells": cells},
+            "config": {"workload": args.workload, "grid": [g["L"], g["M"], g["N"]], "cells": cells,
+                       "plane": [orc.L1, orc.M1], "receivers": orc.NRx, "parallelism": "host cores",
+                       "timed": f"{ran} time steps from a zero state on the host cores"},
             "cpu_baseline": {"value": v, "unit": "Gcell-steps/s", "cores": num_threads(), "kind": "port",
                              "sample": f"{ran} time steps from a zero state, FP64 C restatement of the reference "
                                        f"path (oracle/tcsem_oracle.c), {num_threads()} OpenMP threads"},
