@@ -32,8 +32,9 @@ constexpr int kBndThreads = 256;
 // its own transforms are done (the next one's blocks stage their tables while this one
 // writes its results); the next one waits for this grid's completion and memory before
 // it reads what this grid wrote.  Without the launch attribute the wait returns at once.
-// Releasing the next kernel only at the end keeps its waiting blocks from holding SM
-// resources that the sweep running beside the boundary needs.
+// Releasing the next kernel only after the transforms keeps its waiting blocks from holding
+// SM resources that the sweep running beside the boundary needs.  The last stage releases
+// the top z-chunk of the sweep at its start: by then the sweep's blocks are all resident.
 
 // Natural-spline second derivatives mb[0..n) of the line y[0..n) (stride ys) from
 // the precomputed elimination factors tab = g | w | inv | du (n values each): the
