@@ -122,3 +122,26 @@ def test_one_json_line_per_finished_request(tmp_path):
         q = reqs[r["request"]]
         assert r == json.loads(json.dumps(request_record(q)))
         assert r["latency_s"] == pytest.approx(q.completed - q.arrival) and r["queued_s"] >= 0
+
+
+def test_a_request_stream_drawn_from_a_survey_pool(tmp_path):
+    """make_stream with a pool: seeded Poisson arrivals from 0, one request per arrival, the
+    surveys drawn from `pool` distinct generated input directories, the same stream again
+    from the same seed."""
+    import os
+
+    from tcsem_fdtd_gb300.serve import make_stream
+
+    size = ((64, 64), (64, 64), (48, 48))
+    a = make_stream(12, 8.0, 3, size=size, tn=(1.0, 1.0), root=str(tmp_path / "a"), pool=3)
+    b = make_stream(12, 8.0, 3, size=size, tn=(1.0, 1.0), root=str(tmp_path / "b"), pool=3)
+    assert [r.rid for r in a] == list(range(12))
+    t = [r.arrival for r in a]
+    assert t[0] == 0.0 and all(x <= y for x, y in zip(t, t[1:]))
+    assert [r.arrival for r in b] == t
+    dirs = sorted({r.directory for r in a})
+    assert len(dirs) <= 3 and len(os.listdir(tmp_path / "a")) == 3
+    for d in dirs:
+        assert {"FDTD_setup.in", "Cond.bin", "Receiver.in", "Transmitter.in"} <= set(os.listdir(d))
+    # the same draw of surveys for the same seed
+    assert [os.path.basename(r.directory) for r in a] == [os.path.basename(r.directory) for r in b]
