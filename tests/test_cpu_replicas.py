@@ -60,3 +60,23 @@ def test_reference_arm_under_torchrun_two_ranks():
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
+    assert line["config"]["workload"] == "tiny" and len(line["config"]["plane"]) == 2
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_bench_helpers_on_the_host():
+    """The figures bench.py reads from committed files (the sweep's ncu traffic, the measured HBM
+    peak) and the reference CPU-remap record, which is either a timing or says why it is absent."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from tcsem_fdtd_gb300 import inputs
+
+    t = bench.profiled_traffic("marine3d_256x256x160")
+    assert t is None or 5e8 < t < 7e8  # 575 MB per launch; about 52 B x 10.5 M cells
+    peak, kind = bench.measured_peak()
+    assert peak > 1000 and kind in ("measured", "fallback")
+    d = bench.make_inputs("tiny", 0)
+    rec = bench.reference_cpu_remap(d, reps=2)
+    if rec is not None:
+        L1, M1 = rec["plane"]
+        assert rec["ms_per_call"] > 0 and L1 > 0 and M1 > 0 and rec["kind"] == "reference"
