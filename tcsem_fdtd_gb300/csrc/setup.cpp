@@ -93,6 +93,24 @@ struct Tokens {
 
 }  // namespace
 
+namespace {
+// The grid lines of FDTD_setup.in as the setup (ModelingSetup.cpp:100-152) uses them: strip widths
+// are cell counts (>= 0), each core has at least one cell, the core spacings are positive.  Returns
+// the grid's L, M, N.
+void check_grid(const SurveyInput &in, long &L, long &M, long &N) {
+    const int strips[] = {in.ALx2, in.ALx1, in.ARx1, in.ARx2, in.Ay2, in.Ay1, in.Az2, in.Az1};
+    for (int w : strips)
+        if (w < 0) throw Error(TCSEM_ERR_INVALID, "bad grid dimensions: a negative strip width");
+    if (in.Nx < 1 || in.Ny < 1 || in.Nz < 1) throw Error(TCSEM_ERR_INVALID, "bad grid dimensions: an empty core");
+    if (!(in.dxmin > 0) || !(in.dymin > 0) || !(in.dzmin > 0))
+        throw Error(TCSEM_ERR_INVALID, "bad grid spacing: dxmin, dymin and dzmin must be positive");
+    L = (long)in.ALx2 + in.ALx1 + in.ARx2 + in.ARx1 + in.Nx;
+    M = 2L * (in.Ay2 + in.Ay1) + in.Ny;
+    N = (long)in.Nz + in.Az2 + in.Az1;
+    if (L * M * N > (1L << 33)) throw Error(TCSEM_ERR_INVALID, "bad grid dimensions");
+}
+}  // namespace
+
 SurveyInput read_survey_dir(const std::string &dir) {
     SurveyInput in;
     {  // ModelingSetup.cpp:51-59
@@ -106,8 +124,8 @@ SurveyInput read_survey_dir(const std::string &dir) {
         in.Ay2 = t.get<int>(); in.Ay1 = t.get<int>(); in.Ny = t.get<int>();
         in.Az2 = t.get<int>(); in.Az1 = t.get<int>(); in.Nz = t.get<int>();
     }
-    long L = in.ALx2 + in.ALx1 + in.ARx2 + in.ARx1 + in.Nx, M = 2 * (in.Ay2 + in.Ay1) + in.Ny, N = in.Nz + in.Az2 + in.Az1;
-    if (L < 1 || M < 1 || N < 1 || L * M * N > (1L << 33)) throw Error(TCSEM_ERR_INVALID, "bad grid dimensions");
+    long L, M, N;
+    check_grid(in, L, M, N);
     {  // Cond.bin, float64 [N][M][L] (ModelingSetup.cpp:201-209), read straight into place
         const std::string path = dir + "/Cond.bin";
         std::ifstream f(path, std::ios::binary | std::ios::ate);
@@ -181,8 +199,8 @@ SurveyInput survey_from_host(const tcsem_model *m, const tcsem_survey *s) {
     in.ALx2 = m->ALx2; in.ALx1 = m->ALx1; in.Nx = m->Nx; in.ARx1 = m->ARx1; in.ARx2 = m->ARx2;
     in.Ay2 = m->Ay2; in.Ay1 = m->Ay1; in.Ny = m->Ny;
     in.Az2 = m->Az2; in.Az1 = m->Az1; in.Nz = m->Nz;
-    long L = in.ALx2 + in.ALx1 + in.ARx2 + in.ARx1 + in.Nx, M = 2 * (in.Ay2 + in.Ay1) + in.Ny, N = in.Nz + in.Az2 + in.Az1;
-    if (L < 1 || M < 1 || N < 1 || L * M * N > (1L << 33)) throw Error(TCSEM_ERR_INVALID, "bad grid dimensions");
+    long L, M, N;
+    check_grid(in, L, M, N);
     if (!m->con) throw Error(TCSEM_ERR_INVALID, "null conductivity");
     in.con.assign(m->con, m->con + (size_t)L * M * N);
     in.T0 = s->T0; in.Tn = s->Tn; in.Nt = s->Nt; in.IsLog = s->IsLog;

@@ -105,6 +105,10 @@ def test_in_memory_open_checks_its_records_like_the_parser():
     with pytest.raises(t.TcsemError) as e:
         t.Simulation(model=m2, survey=survey)
     assert e.value.status == 3
+    for bad_grid in (dict(ALx2=-1, Nx=model["Nx"] + 1), dict(Ny=0, Ay1=model["Ay1"] + 1), dict(dzmin=0.0)):
+        with pytest.raises(t.TcsemError) as e:
+            t.Simulation(model=dict(model, **bad_grid), survey=survey)
+        assert e.value.status == 3 and "grid" in str(e.value), bad_grid
     try:
         import torch
 
