@@ -109,6 +109,9 @@ def test_in_memory_open_checks_its_records_like_the_parser():
         with pytest.raises(t.TcsemError) as e:
             t.Simulation(model=dict(model, **bad_grid), survey=survey)
         assert e.value.status == 3 and "grid" in str(e.value), bad_grid
+    with pytest.raises(t.TcsemError) as e:
+        t.Simulation(model=model, survey=dict(survey, Nt=1))
+    assert e.value.status == 3 and "sampling times" in str(e.value)
     try:
         import torch
 
