@@ -61,6 +61,11 @@ typedef struct {
                              the padding UpContinuation.cpp:21-49 sketches): 1 = the powers of two
                              above L1 and M1, 2 = the smallest lengths >= L1, M1 without prime
                              factors above 5; not the reference's arithmetic (default 0) */
+    int persistent_batch; /* batches only: 1 = every block of graph_steps steps of all slots is one
+                             persistent launch whose CTAs take boundary, sweep and receiver items
+                             from a device queue of the stages whose inputs are complete, so each
+                             slot moves on as soon as its own chain allows; default 0 = a captured
+                             graph of one launch per kernel per step for all slots together */
 } tcsem_opts;
 
 typedef struct {
@@ -70,7 +75,9 @@ typedef struct {
     long nsteps;          /* time steps of one transmitter run */
     int precision;
     size_t device_bytes;  /* device memory held by the handle */
-    int launches_per_step; /* kernels launched per time step by tcsem_advance */
+    int launches_per_step; /* kernels launched per time step by tcsem_advance (a batch slot: for
+                              all slots together; 0 with persistent_batch, which launches three
+                              kernels per block of graph_steps steps) */
     int zchunks;          /* z-chunks of the fused sweep in use */
     int top_planes;       /* planes of the top z-chunk when it runs beside the others, else 0 */
     size_t uploaded_bytes; /* host-to-device bytes the open copied (conductivity, grid, boundary and
@@ -266,6 +273,15 @@ tcsem_status tcsem_upcontinuation_noalloc(tcsem_sim_t *sim);
  * stays usable afterwards.  A production kernel that gives up the same way
  * makes the next synchronising call on its handle return TCSEM_ERR_CUDA. */
 tcsem_status tcsem_selftest_bounded_wait(int device, int polls, int *gave_up);
+
+/* Self-test of the bounded wait of the persistent batch schedule (persistent_batch; no
+ * counterpart in the reference): its kernel runs on one CTA of `device` with a queue that
+ * expects one stage and has no slot to publish it, so the CTA's wait for a ready stage gives
+ * up after wait_ns nanoseconds and records that in the schedule's error word, read back into
+ * *gave_up (1 when the wait gave up).  The device stays usable afterwards.  In a batch, a wait
+ * that gives up the same way also marks every slot's error word, and the next tcsem_batch_poll
+ * (or tcsem_batch_traces of a slot) returns TCSEM_ERR_CUDA. */
+tcsem_status tcsem_selftest_queue_wait(int device, long long wait_ns, int *gave_up);
 
 #ifdef __cplusplus
 }

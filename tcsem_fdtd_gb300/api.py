@@ -29,7 +29,7 @@ class TcsemError(RuntimeError):
 class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("fix_dual_bipole", C.c_int), ("graph_steps", C.c_int),
                 ("zchunks", C.c_int), ("serial_boundary", C.c_int), ("top_planes", C.c_int),
-                ("padded_plane", C.c_int)]
+                ("padded_plane", C.c_int), ("persistent_batch", C.c_int)]
 
 
 class Info(C.Structure):
@@ -111,6 +111,7 @@ def library():
         "tcsem_time_steps": (i, [vp, i, l_, dp, dp, dp]),
         "tcsem_timed_advance": (i, [vp, l_, dp]),
         "tcsem_selftest_bounded_wait": (i, [i, i, ip]),
+        "tcsem_selftest_queue_wait": (i, [i, C.c_longlong, ip]),
     }
     sig.update({
         "tcsem_batch_create": (i, [C.POINTER(Opts), C.c_size_t, C.POINTER(vp)]),
@@ -139,6 +140,16 @@ def selftest_bounded_wait(device=0, polls=1000):
     st = library().tcsem_selftest_bounded_wait(device, polls, C.byref(g))
     if st != 0:
         raise TcsemError(st, "bounded-wait self-test failed")
+    return g.value
+
+
+def selftest_queue_wait(device=0, wait_ns=20_000_000):
+    """tcsem_selftest_queue_wait: 1 when the persistent batch kernel's wait for a stage that
+    nothing publishes gave up after wait_ns."""
+    g = C.c_int(0)
+    st = library().tcsem_selftest_queue_wait(device, int(wait_ns), C.byref(g))
+    if st != 0:
+        raise TcsemError(st, "queue-wait self-test failed")
     return g.value
 
 
@@ -342,13 +353,15 @@ class Simulation:
 class Batch:
     """Many surveys advanced together (tcsem_batch_* of include/tcsem.h)."""
 
-    def __init__(self, precision=32, device=0, budget=0, graph_steps=0, zchunks=0, top_planes=0, padded_plane=False):
+    def __init__(self, precision=32, device=0, budget=0, graph_steps=0, zchunks=0, top_planes=0, padded_plane=False,
+                 persistent=False):
         L = library()
         o = Opts()
         L.tcsem_default_opts(C.byref(o))
         o.precision, o.device, o.graph_steps, o.zchunks = precision, device, graph_steps, zchunks
         o.top_planes = top_planes
         o.padded_plane = int(padded_plane)
+        o.persistent_batch = int(persistent)
         h = C.c_void_p()
         st = L.tcsem_batch_create(C.byref(o), int(budget), C.byref(h))
         if st != 0:

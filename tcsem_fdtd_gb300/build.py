@@ -24,7 +24,7 @@ BUILD_CHECK = os.path.join(PKG, "_build_check")
 LIB_CHECK = os.path.join(PKG, "libtcsem_check.so")
 CLI = os.path.join(PKG, "tcsem_fdtd")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["setup.cpp", "volume.cu", "boundary.cu", "rx.cu", "sim.cu", "batch.cu"]
+SOURCES = ["setup.cpp", "volume.cu", "boundary.cu", "rx.cu", "sim.cu", "batch.cu", "persist.cu"]
 
 
 def nvcc():

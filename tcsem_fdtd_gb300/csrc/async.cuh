@@ -34,6 +34,30 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+// the barrier's memory may be reused for other data after this (all its copies have landed)
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// A global load cached in L2 only: for data another CTA of the same launch may have written.
+template <typename T> __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
+// gpu-scope acquire load / release store of a flag or counter in global memory
+__device__ __forceinline__ int ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// gpu-scope fence: with a relaxed atomic after it a release, with a relaxed atomic before it an acquire
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+// orders this thread's generic-proxy accesses of global memory with its bulk copies (async proxy)
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 // Programmatic dependent launch: let the next kernel on the stream start (its blocks become
 // resident and run up to their wait), and wait for the previous kernel's completion and memory.
 // Without the launch attribute on the dependent kernel both are no-ops.

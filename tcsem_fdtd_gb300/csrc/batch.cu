@@ -17,6 +17,7 @@
 // accepted when the estimate of its allocation fits in the batch's budget.
 #include <nvtx3/nvToolsExt.h>
 
+#include "persist.cuh"
 #include "sim_impl.cuh"
 
 namespace tcsem {
@@ -67,6 +68,13 @@ template <typename T> struct BatchImpl : BatchBase {
     static constexpr int kTuneChunks = 3;
     bool tune_pending = false;
     int lay_n = 1, lay_top = 0;
+    // persistent schedule (opts.persistent_batch): one launch per block, items from a device queue
+    bool persistent = false;
+    DevMem pq, pctl, perr;
+    PersistArgs<T> pa{};
+    int pgrid = 0;
+    size_t psmem = 0;
+    static constexpr long long kQueueWaitNs = 2000000000LL;  // a CTA waits at most 2 s for a ready stage
 
     ~BatchImpl() override {
         if (stream) cudaStreamSynchronize(stream);
@@ -97,6 +105,14 @@ template <typename T> struct BatchImpl : BatchBase {
         gsteps = opts.graph_steps > 0 ? opts.graph_steps : 64;
         if (gsteps % 2) gsteps++;
         tune_pending = opts.zchunks < 0;
+        persistent = opts.persistent_batch != 0;
+        if (persistent) {  // queue capacity: every stage of every slot for a block (the tuner's blocks are 8 steps)
+            pq.alloc((size_t)kMaxSlots * kStages * std::max(gsteps, 8) * sizeof(QueueEntry));
+            pctl.alloc(kQWords * sizeof(int));
+            perr.alloc(sizeof(int));
+            CK(cudaMemsetAsync(perr.p, 0, sizeof(int), stream));
+            CK(cudaStreamSynchronize(stream));
+        }
     }
 
     Slot &find(int id) {
@@ -163,6 +179,7 @@ template <typename T> struct BatchImpl : BatchBase {
         smem_bnd[0] = smem_bnd[1] = smem_bnd[2] = 0;
         nmax = 0;
         int *cnt = counters.as<int>();
+        pa = PersistArgs<T>{};
         for (int r = 0; r < n; r++) {
             Slot &s = slots[running[r]];
             SimImpl<T> &m = *s.sim;
@@ -180,6 +197,9 @@ template <typename T> struct BatchImpl : BatchBase {
             ibs[2].off[r + 1] = ibs[2].off[r] + bb.rows_inv;
             ibs[3].off[r + 1] = ibs[3].off[r] + bb.bilinear;
             irs.off[r + 1] = irs.off[r] + rx_blocks(m.rx_stencils());
+            const int it[kStages] = {bb.rows_fwd, bb.cols, bb.rows_inv, (m.g.L + 1) * m.g.M + m.g.L * (m.g.M + 1),
+                                     m.sweep_blocks(), m.rx_stencils()};
+            for (int q = 0; q < kStages; q++) pa.nitems[r][q] = it[q];
             smem_bnd[0] = std::max(smem_bnd[0], bb.smem_rows);
             smem_bnd[1] = std::max(smem_bnd[1], bb.smem_cols);
             smem_bnd[2] = std::max(smem_bnd[2], bb.smem_inv);
@@ -202,6 +222,42 @@ template <typename T> struct BatchImpl : BatchBase {
         CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
         if (std::max({smem_bnd[0], smem_bnd[1], smem_bnd[2], sweep_smem_bytes<T>(nmax)}) > (size_t)maxsm)
             throw Error(TCSEM_ERR_INVALID, "a slot needs more shared memory than a block can have");
+        if (persistent) {  // no graph: the tables above and one launch per block
+            for (int p = 0; p < 2; p++) {
+                pa.sw[p] = dsw[p].as<SweepSlot<T>>();
+                pa.bs[p] = dbs[p].as<BoundarySlot<T>>();
+                pa.rs[p] = drs[p].as<RxSlot<T>>();
+            }
+            pa.q = pq.as<QueueEntry>();
+            pa.ctl = pctl.as<int>();
+            pa.err = perr.as<int>();
+            pa.nslots = n;
+            pa.wait_ns = kQueueWaitNs;
+            const size_t body = rnd16(std::max({smem_bnd[0], smem_bnd[1], smem_bnd[2], sweep_smem_bytes<T>(nmax)}));
+            pa.ctl_off = (int)body;
+            psmem = body + 32;  // the CTA's scheduling words after every body's layout
+            if (psmem > (size_t)maxsm)
+                throw Error(TCSEM_ERR_INVALID, "a slot needs more shared memory than a block can have");
+            CK(persist_configure<T>(psmem));
+            pgrid = persist_blocks<T>(psmem);
+            if (pgrid <= 0) throw Error(TCSEM_ERR_CUDA, "the persistent batch kernel does not fit on the device");
+            // Claims of the boundary stages: about as many per stage as the CTAs each slot has on
+            // average (at least 8), so that a claim carries several rows or columns when many slots
+            // share the GPU; tiles and receiver blocks are claimed one at a time.
+            const int pt = persist_threads(), target = std::max(8, pgrid / n);
+            for (int r = 0; r < n; r++) {
+                for (int q = 0; q < kStages; q++) {
+                    const int ni = pa.nitems[r][q];
+                    int per = 1, units = ni;
+                    if (q < 3) per = (ni + target - 1) / target, units = per ? (ni + per - 1) / per : 0;
+                    if (q == 3) units = std::min((ni + pt - 1) / pt, target);  // output points split evenly
+                    if (q == 5) units = (ni + pt - 1) / pt;
+                    pa.per[r][q] = per;
+                    pa.units[r][q] = units;
+                }
+            }
+            return;
+        }
         // steps alternate the field sets: every slot starts a block in set 0 (blocks have an even length)
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -250,9 +306,9 @@ template <typename T> struct BatchImpl : BatchBase {
             layout(c);
             rebuild();
             if (running.empty()) break;
-            CK(cudaGraphLaunch(gexec, stream));  // untimed
+            launch_block();  // untimed
             CK(cudaEventRecord(e0, stream));
-            CK(cudaGraphLaunch(gexec, stream));
+            launch_block();
             CK(cudaEventRecord(e1, stream));
             CK(cudaEventSynchronize(e1));
             float ms = 0;
@@ -275,7 +331,7 @@ template <typename T> struct BatchImpl : BatchBase {
         if (dirty) rebuild();
         if (running.empty()) return;
         for (long k = 0; k < nsteps; k += gsteps) {
-            CK(cudaGraphLaunch(gexec, stream));
+            launch_block();
             for (int q : running) {
                 Slot &s = slots[q];
                 const bool was = s.finished();
@@ -285,8 +341,43 @@ template <typename T> struct BatchImpl : BatchBase {
         }
     }
 
+    // one block of gsteps steps of every running slot
+    void launch_block() {
+        if (!persistent) {
+            CK(cudaGraphLaunch(gexec, stream));
+            return;
+        }
+        const int n = (int)running.size();
+        int nq = 0;
+        for (int r = 0; r < n; r++) {
+            const Slot &s = slots[running[r]];
+            pa.steps[r] = (int)std::max<long>(0, std::min<long>(gsteps, s.sim->sched.nsteps - s.done));
+            int ns = 0;
+            for (int q = 0; q < kStages; q++) ns += pa.units[r][q] > 0 ? 1 : 0;
+            nq += pa.steps[r] * ns;
+        }
+        pa.nq = nq;
+        if (nq) CK(launch_persistent<T>(pa, pgrid, psmem, stream));
+        launch_advance_all(counters.as<int>(), n, gsteps, stream);
+        CK(cudaGetLastError());
+    }
+
+    // a wait of the persistent schedule that gave up (its slots' error words are set too)
+    void check_schedule() {
+        if (!persistent) return;
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, perr.p, sizeof h, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (h) {
+            CK(cudaMemsetAsync(perr.p, 0, sizeof(int), stream));
+            CK(cudaStreamSynchronize(stream));
+            throw Error(TCSEM_ERR_CUDA, "a wait of the persistent batch schedule gave up");
+        }
+    }
+
     int poll(int *ids, int cap) override {
         CK(cudaStreamSynchronize(stream));
+        check_schedule();
         int c = 0;
         for (auto &s : slots)
             if (s.finished()) {
@@ -306,7 +397,7 @@ template <typename T> struct BatchImpl : BatchBase {
             o->nsteps = s.sim->sched.nsteps;
             o->precision = s.sim->opts.precision;
             o->device_bytes = s.bytes;
-            o->launches_per_step = lps;
+            o->launches_per_step = persistent ? 0 : lps;
             const ZChunks &zc = s.sim->zc;
             o->zchunks = zc.n;
             o->top_planes = zc.n > 1 && zc.kb[1] != (int)(s.sim->model.N / zc.n) ? zc.kb[1] : 0;
@@ -466,6 +557,39 @@ tcsem_status tcsem_batch_remove(tcsem_batch_t *b, int slot) {
 
 tcsem_status tcsem_batch_stats(tcsem_batch_t *b, int *slots, int *running, size_t *device_bytes) {
     return bguard(b, [&](BatchBase &x) { x.stats(slots, running, device_bytes); });
+}
+
+// The persistent batch kernel on one CTA with a queue whose first stage nothing publishes:
+// its wait for a ready stage gives up after wait_ns and sets the schedule's error word.
+tcsem_status tcsem_selftest_queue_wait(int device, long long wait_ns, int *gave_up) {
+    if (!gave_up || wait_ns < 1) return TCSEM_ERR_INVALID;
+    *gave_up = 0;
+    int *words = nullptr;
+    QueueEntry *q = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess || cudaMalloc(&words, (kQWords + 1) * sizeof(int)) != cudaSuccess)
+        return TCSEM_ERR_CUDA;
+    tcsem_status st = TCSEM_OK;
+    if (cudaMalloc(&q, sizeof(QueueEntry)) != cudaSuccess) st = TCSEM_ERR_CUDA;
+    int h = 0;
+    if (st == TCSEM_OK) {
+        PersistArgs<float> a{};
+        a.q = q;
+        a.ctl = words;
+        a.err = words + kQWords;
+        a.nq = 1;       // one stage expected ...
+        a.nslots = 0;   // ... and no slot to publish it
+        a.wait_ns = wait_ns;
+        a.ctl_off = 0;  // no body runs: the scheduling words alone
+        const size_t smem = 64;
+        if (cudaMemset(a.err, 0, sizeof(int)) != cudaSuccess || persist_configure<float>(smem) != cudaSuccess ||
+            launch_persistent<float>(a, 1, smem, nullptr) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+            cudaMemcpy(&h, a.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = TCSEM_ERR_CUDA;
+    }
+    cudaFree(q);
+    cudaFree(words);
+    *gave_up = h;
+    return st;
 }
 
 }  // extern "C"

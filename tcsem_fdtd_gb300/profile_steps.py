@@ -2,7 +2,7 @@
 
     python -m tcsem_fdtd_gb300.profile_steps [--workload marine3d_256x256x160] [--steps 16]
                                              [--precision 32] [--serial-boundary] [--fused N]
-                                             [--batch N]
+                                             [--batch N [--persistent]]
 
 Writes the workload's input files to a temporary directory, opens it through
 the C ABI and advances `--steps` steps (CUDA graphs of 8 steps), then exits.
@@ -10,7 +10,8 @@ With `--fused N` it instead launches the fused sweep alone N times
 (tcsem_fused_step: every z-chunk of the default layout in one launch, the
 launch bench.py times for the roofline).  With `--batch N` it advances a
 batch of the first N generated surveys of the batched workload instead
-(`--steps` steps, graph blocks of 8).
+(`--steps` steps, graph blocks of 8; with `--persistent` each block is one
+launch of the persistent batch kernel).
 It reports nothing about speed: time with bench.py, and use this under ncu to
 get a launch list or a capture of one kernel on a short run.
 """
@@ -33,6 +34,7 @@ def main(argv=None):
                     help="boundary pipeline before one launch of the whole sweep (no overlap)")
     ap.add_argument("--fused", type=int, default=0, help="launch the fused sweep alone this many times")
     ap.add_argument("--batch", type=int, default=0, help="advance a batch of this many generated surveys")
+    ap.add_argument("--persistent", action="store_true", help="the batch's persistent schedule (one launch per block)")
     a = ap.parse_args(argv)
     if a.batch:
         from tcsem_fdtd_gb300 import Batch
@@ -43,7 +45,7 @@ def main(argv=None):
             dq = os.path.join(root, f"s{q:03d}")
             inputs.write_case(inputs.batch_case(q), dq)
             dirs.append(dq)
-        with Batch(precision=a.precision, graph_steps=8) as b:
+        with Batch(precision=a.precision, graph_steps=8, persistent=a.persistent) as b:
             for dq in dirs:
                 b.add(dq)
             b.advance(a.steps)

@@ -31,7 +31,7 @@ def test_opts_and_info_struct_layout_matches_header():
     o = Opts()
     t.library().tcsem_default_opts(C.byref(o))
     assert o.precision == 32 and o.device == 0 and o.fix_dual_bipole == 0 and o.serial_boundary == 0
-    assert C.sizeof(Opts) == 32
+    assert C.sizeof(Opts) == 36 and o.persistent_batch == 0
 
 
 def test_struct_offsets_match_the_c_compiler(tmp_path):

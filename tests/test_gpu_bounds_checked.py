@@ -4,7 +4,8 @@ The library built with -DTCSEM_CHECK (tcsem_fdtd_gb300/build.py build_check,
 csrc/check.cuh) tests every computed global index of the kernels against its
 array and records a miss in the device error word, which any later call turns
 into TCSEM_ERR_CUDA.  The same runs -- whole runs in both precisions and step
-orders, several z-chunk layouts, the stage entry points and a batch -- go
+orders, several z-chunk layouts, the stage entry points and a batch under
+both schedules (per-kernel graph and persistent kernel) -- go
 through the normal and the checked library in separate processes: the checked
 one must report no miss, and its outputs must equal the normal library's bit
 for bit (the checks never change the arithmetic).
@@ -47,13 +48,14 @@ for name, d in cases.items():
         sim.synchronize()  # reads the device error word
         for f in ("Ex", "Ey", "Ez", "Bx", "By", "Bz", "BxAir", "ByAir"):
             out[f"{name}_stage_{f}"] = sim.get(f)
-with Batch(precision=32) as b:
-    slots = [b.add(d) for d in cases.values()]
-    while b.stats()["running"]:
-        b.advance(64)
-    b.poll()
-    for n, s in zip(cases, slots):
-        out[f"{n}_batch"] = b.traces(s)
+for tag, persistent in (("batch", False), ("persistent", True)):
+    with Batch(precision=32, persistent=persistent) as b:
+        slots = [b.add(d) for d in cases.values()]
+        while b.stats()["running"]:
+            b.advance(64)
+        b.poll()
+        for n, s in zip(cases, slots):
+            out[f"{n}_{tag}"] = b.traces(s)
 np.savez(__OUT__, **out)
 """
 
