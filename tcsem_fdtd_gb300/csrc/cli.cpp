@@ -3,7 +3,8 @@
 // working directory (or the directory given as the first argument), runs every
 // transmitter and writes Tx<k>.bout and testwaveform.dat like main.cu:58-324.
 // Options: --fp64 (double-precision build mode), --device N, --fix-dual-bipole,
-// --batch (all transmitters advanced together as one device batch), --padded-plane /
+// --batch (all transmitters advanced together as one device batch; --persistent: its
+// persistent schedule, one launch per block of steps), --padded-plane /
 // --smooth-plane (air field continued on a power-of-two / 5-smooth plane with tapered
 // edges; not the reference's arithmetic).
 #include <chrono>
@@ -23,14 +24,15 @@ int main(int argc, char **argv) {
     for (int a = 1; a < argc; a++) {
         if (!std::strcmp(argv[a], "--fp64")) o.precision = TCSEM_FP64;
         else if (!std::strcmp(argv[a], "--batch")) batch = true;
+        else if (!std::strcmp(argv[a], "--persistent")) o.persistent_batch = 1;
         else if (!std::strcmp(argv[a], "--fix-dual-bipole")) o.fix_dual_bipole = 1;
         else if (!std::strcmp(argv[a], "--padded-plane")) o.padded_plane = 1;
         else if (!std::strcmp(argv[a], "--smooth-plane")) o.padded_plane = 2;
         else if (!std::strcmp(argv[a], "--device") && a + 1 < argc) o.device = std::atoi(argv[++a]);
         else if (argv[a][0] != '-') dir = argv[a];
         else {
-            std::fprintf(stderr, "usage: tcsem_fdtd [dir] [--fp64] [--device N] [--fix-dual-bipole] [--batch] "
-                                 "[--padded-plane | --smooth-plane]\n");
+            std::fprintf(stderr, "usage: tcsem_fdtd [dir] [--fp64] [--device N] [--fix-dual-bipole] "
+                                 "[--batch [--persistent]] [--padded-plane | --smooth-plane]\n");
             return 2;
         }
     }

@@ -48,13 +48,15 @@ class Request:
 class Server:
     """Continuous batching of survey requests on one GPU."""
 
-    def __init__(self, precision=32, device=0, budget=64 << 30, block=64, zchunks=0, batch=None):
+    def __init__(self, precision=32, device=0, budget=64 << 30, block=64, zchunks=0, batch=None, persistent=False):
         """`batch`: an object with the methods of :class:`~tcsem_fdtd_gb300.api.Batch` used here
-        (add, advance, poll, info, traces, remove, close); a device batch by default."""
+        (add, advance, poll, info, traces, remove, close); a device batch by default, with the
+        persistent schedule (one launch per block) when `persistent`."""
         if batch is None:
             from .api import Batch
 
-            batch = Batch(precision=precision, device=device, budget=budget, graph_steps=block, zchunks=zchunks)
+            batch = Batch(precision=precision, device=device, budget=budget, graph_steps=block, zchunks=zchunks,
+                          persistent=persistent)
         self.batch = batch
         self.block = block
         self.queue, self.running, self.done = [], {}, []
@@ -187,12 +189,13 @@ def main(argv=None):
     ap.add_argument("--plain", action="store_true", help="also serve the stream one request at a time")
     ap.add_argument("--jsonl", default=None, help="write one JSON line per finished request to this file")
     ap.add_argument("--pool", type=int, default=0, help="distinct surveys the requests draw from (0: one each)")
+    ap.add_argument("--persistent", action="store_true", help="the batch's persistent schedule (one launch per block)")
     a = ap.parse_args(argv)
     from . import build
 
     build.build()
     reqs = make_stream(a.requests, a.rate, a.seed, tn=tuple(a.tn), pool=a.pool)
-    srv = Server(budget=int(a.budget_gb * (1 << 30)), block=a.block)
+    srv = Server(budget=int(a.budget_gb * (1 << 30)), block=a.block, persistent=a.persistent)
     log = open(a.jsonl, "w") if a.jsonl else None
     try:
         out = {"batched": summary(reqs, serve(reqs, srv, log=log))}

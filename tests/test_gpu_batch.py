@@ -135,17 +135,19 @@ def test_admission_by_device_budget(built, case_dir):
 
 
 def test_cli_batch_mode_writes_the_same_files(built, case_dir, tmp_path):
-    """tcsem_fdtd --batch (all transmitters as one batch) writes the same Tx<k>.bout as the serial CLI."""
+    """tcsem_fdtd --batch (all transmitters as one batch, with either schedule) writes the same
+    Tx<k>.bout as the serial CLI."""
     import shutil
     import subprocess
 
     from tcsem_fdtd_gb300 import build
 
     out = {}
-    for mode in ("serial", "batch"):
+    flags = {"serial": [], "batch": ["--batch"], "persistent": ["--batch", "--persistent"]}
+    for mode in flags:
         d = tmp_path / mode
         shutil.copytree(case_dir("txvar"), d)
-        args = [build.CLI, str(d)] + (["--batch"] if mode == "batch" else [])
+        args = [build.CLI, str(d)] + flags[mode]
         r = subprocess.run(args, capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
         out[mode] = {}
@@ -154,6 +156,7 @@ def test_cli_batch_mode_writes_the_same_files(built, case_dir, tmp_path):
             hdr = tuple(int(v) for v in np.frombuffer(raw[:12], np.int32))
             out[mode][k] = (hdr, np.frombuffer(raw[12:], np.float64).reshape(hdr))
     for k in range(1, 7):
-        (h1, a), (h2, b) = out["serial"][k], out["batch"][k]
-        assert h1 == h2
+        (h1, a), (h2, b), (h3, c) = out["serial"][k], out["batch"][k], out["persistent"][k]
+        assert h1 == h2 == h3
         assert rel_err(b, a) <= 1e-4  # FP32; one z-chunk per batch slot vs the single-survey layout
+        assert rel_err(c, b) <= 1e-6  # the same slots under the two schedules
