@@ -38,8 +38,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
 __device__ __forceinline__ void mbar_inval(uint64_t *bar) {
     asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// A global load cached in L2 only: for data another CTA of the same launch may have written.
-template <typename T> __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
+// A load of data an earlier kernel wrote (FRESH = false: through the read-only cache) or that
+// another CTA of the same launch may have written (FRESH = true: cached in L2 only).
+template <bool FRESH, typename T> __device__ __forceinline__ T ld_in(const T *p) {
+    if constexpr (FRESH) return __ldcg(p);
+    else return __ldg(p);
+}
 // gpu-scope acquire load / release store of a flag or counter in global memory
 __device__ __forceinline__ int ld_acquire(const int *p) {
     int v;

@@ -173,9 +173,9 @@ __device__ __forceinline__ void pad_line(C2<T> *a, int n, int nu, int d, const T
 // j0+1 travel as the real and imaginary parts of one complex transform and are
 // separated in the spectrum: X1 = (Z[k] + conj Z[-k]) / 2, X2 = (Z[k] - conj Z[-k]) / 2i.
 // Output FT is stored x-frequency major, FT[kx][j].
-template <typename T>
-__device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *bz,
-                                             const T *tot, int nch, const Geom &g, int blk) {
+template <typename T, bool FRESH = false>  // FRESH: bz and tot may come from this launch (persistent schedule)
+__device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *__restrict__ bz,
+                                             const T *__restrict__ tot, int nch, const Geom &g, int blk) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int L1 = bd.L1, L = g.L;
     const AxisRemap<T> &R = bd.rx;
@@ -209,8 +209,8 @@ __device__ __forceinline__ void rows_fwd_cta(const BoundaryDev<T> &bd, const T *
             const long long o = (long long)(j0 + r + 1) * g.XP + 4 + i;
             T p[kMaxChunks];
 #pragma unroll
-            for (int c = 1; c < kMaxChunks; c++) p[c] = c < nch ? tot[c * plane + o] : T(0);
-            v = bz[plane + o];
+            for (int c = 1; c < kMaxChunks; c++) p[c] = c < nch ? ld_in<FRESH>(tot + c * plane + o) : T(0);
+            v = ld_in<FRESH>(bz + plane + o);
 #pragma unroll
             for (int c = 1; c < kMaxChunks; c++)
                 if (c < nch) v += p[c];

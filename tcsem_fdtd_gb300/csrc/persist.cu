@@ -117,7 +117,7 @@ template <typename T> __device__ int run_item(const PersistArgs<T> &a, const int
                 __syncthreads();
                 if (threadIdx.x == 0) mbar_inval(reinterpret_cast<uint64_t *>(smem_raw));
             }
-            if (stage == 0) rows_fwd_cta<T>(d->bd, d->bz, d->tot, d->nch, d->g, b);
+            if (stage == 0) rows_fwd_cta<T, true>(d->bd, d->bz, d->tot, d->nch, d->g, b);
             else if (stage == 1) cols_cta<T>(d->bd, b);
             else rows_inv_cta<T>(d->bd, b);
         }
@@ -128,7 +128,7 @@ template <typename T> __device__ int run_item(const PersistArgs<T> &a, const int
         const long st = (long)*d.step_base + step;
         if (st >= d.nsteps) return 0;
         const int bx = u % d.tiles_x, rest = u / d.tiles_x, by = rest % d.tiles_y, c = rest / d.tiles_y;
-        sweep_cta<T>(d.maps, d.g, d.out, d.tin, d.tout, d.ax, d.table[st], d.src, d.zc, bx, by, c, d.err);
+        sweep_cta<T, true>(d.maps, d.g, d.out, d.tin, d.tout, d.ax, d.table[st], d.src, d.zc, bx, by, c, d.err);
         return 2;
     }
     default: {

@@ -321,10 +321,11 @@ __device__ __forceinline__ bool sweep_march(SweepThread<T> &t, const StepScalars
     return ok;
 }
 
-// one CTA of the sweep: tile (bx, by) of z-chunk c with the step scalars s
-template <typename T>
+// one CTA of the sweep: tile (bx, by) of z-chunk c with the step scalars s.  FRESH: the chunk
+// totals tin may have been written by another CTA of the same launch (persistent schedule).
+template <typename T, bool FRESH = false>
 __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, const FieldSet<T> &out,
-                                          const T *tin, T *tout, const Axis<T> &ax,
+                                          const T *__restrict__ tin, T *__restrict__ tout, const Axis<T> &ax,
                                           StepScalars<T> s, const SourceTable<T> &src, const ZChunks &zc, int bx,
                                           int by, int c, int *err) {
     using namespace fs3;
@@ -431,8 +432,8 @@ __device__ __forceinline__ void sweep_cta(const SweepMaps &maps, const Geom &g, 
                 T pv[kMaxChunks];  // all loads in flight together
 #pragma unroll
                 for (int q = 1; q < kMaxChunks; q++)
-                    pv[q] = q > c && q < zc.n && TCSEM_IN(q * t.PS + pc, zc.n * t.PS, err) ? ld_cg(tin + q * t.PS + pc) : T(0);
-                const T first = c + 1 < zc.n ? ld_cg(tin + (c + 1) * t.PS + pc) : T(0);
+                    pv[q] = q > c && q < zc.n && TCSEM_IN(q * t.PS + pc, zc.n * t.PS, err) ? ld_in<FRESH>(tin + q * t.PS + pc) : T(0);
+                const T first = c + 1 < zc.n ? ld_in<FRESH>(tin + (c + 1) * t.PS + pc) : T(0);
 #pragma unroll
                 for (int q = 1; q < kMaxChunks; q++)
                     if (q > c && q < zc.n) o += pv[q];
