@@ -42,10 +42,21 @@ __global__ void k_advance_all(int *counters, int n, int by) {
 
 template <typename T>
 void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const T *tot, const ZChunks &zc, const Geom &g, StepGate gate,
-               RxAction act, cudaStream_t st) {
+               RxAction act, cudaStream_t st, bool early) {
     int n = rd.NComp * rd.nr;
     if (n == 0) return;
-    k_rx<T><<<rx_blocks(n), kRxThreads, 0, st>>>(rd, f, tot, zc, g, gate, act);
+    // early: programmatic dependent launch after the previous kernel on the stream, for receivers
+    // that read nothing that kernel writes (they do not wait for it; its launch latency is saved)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(rx_blocks(n));
+    cfg.blockDim = dim3(kRxThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = early ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_rx<T>, rd, f, tot, zc, g, gate, act);
 }
 
 void launch_advance(int *base, int by, cudaStream_t st) { k_advance<float><<<1, 1, 0, st>>>(base, by); }
@@ -58,9 +69,9 @@ template <typename T> void launch_rx_batched(const RxSlot<T> *slots, const Batch
 }
 
 template void launch_rx<float>(const RxDev<float> &, FieldSet<float>, const float *, const ZChunks &, const Geom &,
-                               StepGate, RxAction, cudaStream_t);
+                               StepGate, RxAction, cudaStream_t, bool);
 template void launch_rx<double>(const RxDev<double> &, FieldSet<double>, const double *, const ZChunks &, const Geom &,
-                                StepGate, RxAction, cudaStream_t);
+                                StepGate, RxAction, cudaStream_t, bool);
 template void launch_rx_batched<float>(const RxSlot<float> *, const BatchIndex &, int, cudaStream_t);
 template void launch_rx_batched<double>(const RxSlot<double> *, const BatchIndex &, int, cudaStream_t);
 

@@ -27,7 +27,7 @@ template <typename T> struct RxDev {
 
 template <typename T>
 void launch_rx(const RxDev<T> &rd, FieldSet<T> f, const T *tot, const ZChunks &zc, const Geom &g, StepGate gate,
-               RxAction act, cudaStream_t st);
+               RxAction act, cudaStream_t st, bool early = false);
 void launch_advance(int *base, int by, cudaStream_t st);
 
 constexpr int kRxThreads = 128;

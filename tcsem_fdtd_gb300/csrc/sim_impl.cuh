@@ -749,10 +749,10 @@ template <typename T> struct SimImpl : SimBase {
     // opens with nothing pending and closes by launching the receivers of its last step (the
     // step counter advance comes after them).
     void rx_open() { rx_pending = -1; }
-    void rx_close() {
+    void rx_close(bool early = false) {
         if (overlap && rx_pending >= 0) {
             launch_rx<T>(rd, fs(rx_pending), tot[rx_pending].as<T>(), zc, g, rx_gate, RxAction{-1, 0, 0, -1, 0, 0},
-                         stream);
+                         stream, early);
             rx_pending = -1;
         }
     }
@@ -769,7 +769,9 @@ template <typename T> struct SimImpl : SimBase {
             // while the bilinear remap runs and waits for it only before the air plane
             sweep(b, StepScalars<T>{}, table, gate, 0, 1, side, true);
             sweep(b, StepScalars<T>{}, table, gate, 1, zc.n, stream);
-            rx_close();  // set b, which this step only reads (receiver stencils never reach the air plane)
+            // set b, which this step only reads (receiver stencils never reach the air plane); launched as
+            // a programmatic dependent of the lower chunks, whose output it does not read
+            rx_close(true);
             CK(cudaEventRecord(ev_join, side));
             CK(cudaStreamWaitEvent(stream, ev_join, 0));
             rx_pending = b ^ 1;
